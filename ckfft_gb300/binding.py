@@ -1,0 +1,157 @@
+"""ctypes binding of libckfft_cuda.so (include/ckfft_cuda.h).
+
+This is plumbing for Python callers, tests and the benchmark: every call goes
+through the C ABI into the CUDA kernels.  There is no Python or CPU fallback;
+if the library is missing, `load()` raises.
+
+Arrays may be numpy arrays (host memory) or torch tensors (host or CUDA);
+anything exposing a data pointer works through the raw `call_*` helpers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libckfft_cuda.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "ckfft_cuda.h")
+
+FORWARD, INVERSE, BOTH = 1, 2, 3
+
+_lib = None
+
+
+class CkFftError(RuntimeError):
+    """A CkFft call returned 0 / NULL; the message is CkFftCudaGetLastError()."""
+
+
+def header_functions() -> list[str]:
+    """Names of the functions declared in include/ckfft_cuda.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b(CkFft\w+)\s*\(", text)
+    seen = []
+    for n in names:
+        if n not in seen:
+            seen.append(n)
+    return seen
+
+
+def load(path: str | None = None):
+    """Loads (once) and returns the CDLL with argument types declared."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"{p} is missing: build it with `python -m ckfft_gb300.build`")
+    lib = C.CDLL(p)
+    vp, i, sz = C.c_void_p, C.c_int, C.c_size_t
+    lib.CkFftInit.restype = vp
+    lib.CkFftInit.argtypes = [i, i, vp, C.POINTER(sz)]
+    lib.CkFftShutdown.restype = None
+    lib.CkFftShutdown.argtypes = [vp]
+    for f in ("CkFftComplexForward", "CkFftComplexInverse", "CkFftRealForward"):
+        getattr(lib, f).restype = i
+        getattr(lib, f).argtypes = [vp, i, vp, vp]
+    lib.CkFftRealInverse.restype = i
+    lib.CkFftRealInverse.argtypes = [vp, i, vp, vp, vp]
+    lib.CkFftCudaGetLastError.restype = C.c_char_p
+    lib.CkFftCudaGetLastError.argtypes = []
+    for f in ("CkFftCudaComplexForwardBatch", "CkFftCudaComplexInverseBatch",
+              "CkFftCudaRealForwardBatch", "CkFftCudaRealInverseBatch"):
+        getattr(lib, f).restype = i
+        getattr(lib, f).argtypes = [vp, i, i, vp, vp, vp]
+    lib.CkFftCudaLaunchCount.restype = C.c_longlong
+    lib.CkFftCudaLaunchCount.argtypes = []
+    _declare_extras(lib)
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _declare_extras(lib):
+    """Argument types of the later additions to the header, when present."""
+    vp, i, ll = C.c_void_p, C.c_int, C.c_longlong
+    if hasattr(lib, "CkFftCudaRunJobs"):
+        lib.CkFftCudaRunJobs.restype = i
+        lib.CkFftCudaRunJobs.argtypes = [vp, vp, i, vp]
+
+
+def last_error() -> str:
+    return load().CkFftCudaGetLastError().decode(errors="replace")
+
+
+def ptr(a) -> int | None:
+    """Raw data pointer of a numpy array or torch tensor (None passes NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if hasattr(a, "ctypes"):
+        return a.ctypes.data
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+def launch_count() -> int:
+    return load().CkFftCudaLaunchCount()
+
+
+class Context:
+    """Owns one CkFftContext (CkFftInit / CkFftShutdown)."""
+
+    def __init__(self, nmax: int, direction: int = BOTH):
+        self.lib = load()
+        self.nmax = nmax
+        self.direction = direction
+        self.handle = self.lib.CkFftInit(nmax, direction, None, None)
+        if not self.handle:
+            raise CkFftError(f"CkFftInit({nmax}, {direction}) failed: {last_error()}")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.CkFftShutdown(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- raw calls: pointers in, return code out (1 ok, 0 invalid/failed)
+    def complex_forward(self, n, inp, out) -> int:
+        return self.lib.CkFftComplexForward(self.handle, n, ptr(inp), ptr(out))
+
+    def complex_inverse(self, n, inp, out) -> int:
+        return self.lib.CkFftComplexInverse(self.handle, n, ptr(inp), ptr(out))
+
+    def real_forward(self, n, inp, out) -> int:
+        return self.lib.CkFftRealForward(self.handle, n, ptr(inp), ptr(out))
+
+    def real_inverse(self, n, inp, out, tmp) -> int:
+        return self.lib.CkFftRealInverse(self.handle, n, ptr(inp), ptr(out), ptr(tmp))
+
+    def batch(self, kind: str, n: int, count: int, inp, out, stream=None) -> int:
+        """kind: 'cfwd', 'cinv', 'rfwd', 'rinv'; stream: cudaStream_t as int or a torch stream."""
+        fn = {
+            "cfwd": self.lib.CkFftCudaComplexForwardBatch,
+            "cinv": self.lib.CkFftCudaComplexInverseBatch,
+            "rfwd": self.lib.CkFftCudaRealForwardBatch,
+            "rinv": self.lib.CkFftCudaRealInverseBatch,
+        }[kind]
+        s = getattr(stream, "cuda_stream", stream)
+        return fn(self.handle, n, count, ptr(inp), ptr(out), s)
+
+    def check(self, rc: int, what: str = "call"):
+        if rc != 1:
+            raise CkFftError(f"{what} failed: {last_error()}")

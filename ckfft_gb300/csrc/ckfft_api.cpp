@@ -1,0 +1,547 @@
+// ckfft_api.cpp -- the C ABI (include/ckfft_cuda.h) over the CUDA kernels.
+//
+// Mirrors the reference's API layer (src/ckfft/ckfft.cpp:14-119): the same
+// argument checks in the same order with the same 0 / NULL results, and the
+// context rules of src/ckfft/context.cpp:45-143 (size query through bufSize,
+// caller-provided memory, Shutdown freeing only what Init allocated).
+// Instead of FP32 tables in host memory the context owns FP64-derived
+// twiddle tables in device memory, and every transform runs as CUDA kernels.
+//
+// Pointer handling: device and managed pointers on the context's device are
+// used in place; host pointers (pageable or pinned) are moved through
+// device-resident staging buffers, split into chunks that run on three
+// streams so that host->device copies, kernels and device->host copies of
+// consecutive chunks overlap.
+#include "ckfft_cuda.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace ckg {
+void build_twiddles(int log2n, std::vector<float2>& tab);
+}
+
+namespace {
+
+thread_local std::string t_error;
+
+void set_error(const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_error = buf;
+}
+
+int fail(const char* what)
+{
+    set_error("%s", what);
+    return 0;
+}
+
+int cuda_fail(const char* where, cudaError_t e)
+{
+    set_error("%s: %s", where, cudaGetErrorString(e));
+    return 0;
+}
+
+// isPowerOfTwo of src/ckfft/math_util.h:12-15, applied to the int the caller
+// passed.  Values <= 0 are rejected too (the reference lets INT_MIN through
+// this test and then misbehaves).
+bool valid_size(int n, int nmax)
+{
+    if (n <= 0) return false;
+    const unsigned u = (unsigned)n;
+    return (u & (u - 1)) == 0 && n <= nmax;
+}
+
+int log2i(long long n)
+{
+    int l = 0;
+    while ((1ll << l) < n) ++l;
+    return l;
+}
+
+constexpr int kSlots = 3;
+constexpr size_t kChunkBytes = 64ull << 20;   // per staging buffer
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    void* din = nullptr;
+    size_t din_cap = 0;
+    void* dout = nullptr;
+    size_t dout_cap = 0;
+};
+
+struct Lane {
+    Slot slot[kSlots];
+    void* scratch = nullptr;
+    size_t scratch_cap = 0;
+    bool busy = false;
+};
+
+struct LanePool {
+    std::mutex mu;
+    std::vector<Lane*> lanes;
+};
+
+constexpr uint32_t kMagic = 0x43554646u;   // "CUFF"
+
+}  // namespace
+
+struct _CkFftContext {
+    uint32_t magic;
+    int nmax;
+    int log2max;
+    int direction;
+    int device;
+    int own_buf;
+    float2* dtw;            // twiddle levels, 2 * nmax entries
+    LanePool* pool;
+};
+
+namespace {
+
+// Keeps the context's device current for the duration of a call.
+struct DeviceScope {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceScope(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) { ok = false; return; }
+        if (prev != dev && cudaSetDevice(dev) != cudaSuccess) ok = false;
+    }
+    ~DeviceScope()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+Lane* acquire_lane(CkFftContext* c)
+{
+    std::lock_guard<std::mutex> lock(c->pool->mu);
+    for (Lane* l : c->pool->lanes) {
+        if (!l->busy) { l->busy = true; return l; }
+    }
+    Lane* l = new (std::nothrow) Lane();
+    if (!l) return nullptr;
+    for (int i = 0; i < kSlots; ++i) {
+        if (cudaStreamCreateWithFlags(&l->slot[i].stream, cudaStreamNonBlocking) != cudaSuccess) {
+            for (int j = 0; j < i; ++j) cudaStreamDestroy(l->slot[j].stream);
+            delete l;
+            return nullptr;
+        }
+    }
+    l->busy = true;
+    c->pool->lanes.push_back(l);
+    return l;
+}
+
+void release_lane(CkFftContext* c, Lane* l)
+{
+    std::lock_guard<std::mutex> lock(c->pool->mu);
+    l->busy = false;
+}
+
+void free_lane(Lane* l)
+{
+    for (int i = 0; i < kSlots; ++i) {
+        if (l->slot[i].stream) cudaStreamSynchronize(l->slot[i].stream);
+        cudaFree(l->slot[i].din);
+        cudaFree(l->slot[i].dout);
+        if (l->slot[i].stream) cudaStreamDestroy(l->slot[i].stream);
+    }
+    cudaFree(l->scratch);
+    delete l;
+}
+
+cudaError_t grow(void** p, size_t* cap, size_t need)
+{
+    if (*cap >= need) return cudaSuccess;
+    cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(p, need);
+    if (e == cudaSuccess) *cap = need;
+    return e;
+}
+
+enum class Mem { Host, Device };
+
+// Classifies a pointer; returns false (with an error set) for device memory
+// that belongs to another device.
+bool classify(const void* p, int dev, Mem* where)
+{
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *where = Mem::Host;
+        return true;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+        if (a.type == cudaMemoryTypeDevice && a.device != dev) {
+            set_error("pointer %p is device memory of device %d, context is on device %d", p, a.device, dev);
+            return false;
+        }
+        *where = Mem::Device;
+        return true;
+    }
+    *where = Mem::Host;
+    return true;
+}
+
+// One transform family request.
+struct Work {
+    ckg::Kind kind;
+    int n;
+    int log2n;
+    long long count;
+    size_t in_bytes;        // per transform
+    size_t out_bytes;
+    long long in_dist;      // elements of the input type between transforms
+    long long out_dist;
+};
+
+Work make_work(ckg::Kind kind, int n, long long count)
+{
+    Work w;
+    w.kind = kind;
+    w.n = n;
+    w.log2n = log2i(n);
+    w.count = count;
+    const size_t cplx = sizeof(CkFftComplex);
+    switch (kind) {
+    case ckg::C2C_FWD:
+    case ckg::C2C_INV:
+        w.in_bytes = w.out_bytes = cplx * (size_t)n;
+        w.in_dist = w.out_dist = n;
+        break;
+    case ckg::R2C:
+        w.in_bytes = sizeof(float) * (size_t)n;
+        w.out_bytes = cplx * (size_t)(n / 2 + 1);
+        w.in_dist = n;
+        w.out_dist = n / 2 + 1;
+        break;
+    case ckg::C2R:
+        w.in_bytes = cplx * (size_t)(n / 2 + 1);
+        w.out_bytes = sizeof(float) * (size_t)n;
+        w.in_dist = n / 2 + 1;
+        w.out_dist = n;
+        break;
+    }
+    return w;
+}
+
+bool is_real(ckg::Kind k) { return k == ckg::R2C || k == ckg::C2R; }
+
+bool needs_large(const Work& w)
+{
+    return is_real(w.kind) ? w.log2n > ckg::kSmallMaxLog2Real : w.log2n > ckg::kSmallMaxLog2Complex;
+}
+
+// Enqueues the kernels for `cnt` transforms between device buffers.
+// `scratch` must hold large_scratch_bytes() * cnt bytes when the size needs
+// the multi-pass path (a smaller scratch runs the batch in groups).
+cudaError_t enqueue(const CkFftContext* c, const Work& w, long long cnt, const void* din, void* dout,
+                    void* scratch, size_t scratch_bytes, cudaStream_t s)
+{
+    if (cnt <= 0) return cudaSuccess;
+    if (is_real(w.kind) && w.n <= 4)
+        return ckg::launch_real_tiny(w.kind, w.n, din, dout, cnt, w.in_dist, w.out_dist, s);
+    if (!needs_large(w))
+        return ckg::launch_small(w.kind, w.log2n, din, dout, cnt, w.in_dist, w.out_dist, c->dtw, s);
+    switch (w.kind) {
+    case ckg::C2C_FWD:
+    case ckg::C2C_INV:
+        return ckg::launch_large_c2c(w.kind == ckg::C2C_INV, w.log2n, din, dout, cnt, w.in_dist, w.out_dist,
+                                     c->dtw, scratch, scratch_bytes, s);
+    case ckg::R2C:
+        return ckg::launch_large_r2c(w.log2n, din, dout, cnt, w.in_dist, w.out_dist, c->dtw, scratch,
+                                     scratch_bytes, s);
+    case ckg::C2R:
+        return ckg::launch_large_c2r(w.log2n, din, dout, cnt, w.in_dist, w.out_dist, c->dtw, scratch,
+                                     scratch_bytes, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// Scratch for the multi-pass path: enough for a group of transforms whose
+// intermediate stays within a bounded size (at least one transform).
+size_t scratch_need(const Work& w, long long cnt)
+{
+    if (!needs_large(w)) return 0;
+    const size_t one = ckg::large_scratch_bytes(w.kind, w.log2n);
+    const size_t cap = 256ull << 20;
+    long long g = (long long)(cap / one);
+    if (g < 1) g = 1;
+    if (g > cnt) g = cnt;
+    return one * (size_t)g;
+}
+
+// Runs a request.  stream != NULL with device pointers: asynchronous on that
+// stream.  Otherwise blocking, through a lane of the context's pool.
+int run(CkFftContext* c, const Work& w, const void* in, void* out, cudaStream_t user_stream,
+        void* user_scratch = nullptr, size_t user_scratch_bytes = 0)
+{
+    DeviceScope scope(c->device);
+    if (!scope.ok) return fail("cannot select the context's CUDA device");
+    if (w.count == 0) return 1;
+    Mem min, mout;
+    if (!classify(in, c->device, &min) || !classify(out, c->device, &mout)) return 0;
+
+    if (user_stream && min == Mem::Device && mout == Mem::Device) {
+        // asynchronous path: scratch from the stream-ordered allocator
+        const size_t need = scratch_need(w, w.count);
+        void* scratch = nullptr;
+        if (need) {
+            cudaError_t e = cudaMallocAsync(&scratch, need, user_stream);
+            if (e != cudaSuccess) return cuda_fail("cudaMallocAsync(scratch)", e);
+        }
+        cudaError_t e = enqueue(c, w, w.count, in, out, scratch, need, user_stream);
+        if (scratch) cudaFreeAsync(scratch, user_stream);
+        if (e != cudaSuccess) return cuda_fail("kernel launch", e);
+        return 1;
+    }
+
+    Lane* lane = acquire_lane(c);
+    if (!lane) return fail("cannot create a staging lane (CUDA streams)");
+    int ok = 1;
+    cudaError_t e = cudaSuccess;
+    const char* where = "";
+    // a user stream orders the blocking call after the stream's earlier work
+    cudaEvent_t dep = nullptr;
+    if (user_stream) {
+        if ((e = cudaEventCreateWithFlags(&dep, cudaEventDisableTiming)) != cudaSuccess) { where = "cudaEventCreate"; goto done; }
+        if ((e = cudaEventRecord(dep, user_stream)) != cudaSuccess) { where = "cudaEventRecord"; goto done; }
+        for (int i = 0; i < kSlots; ++i) cudaStreamWaitEvent(lane->slot[i].stream, dep, 0);
+    }
+    {
+        const size_t per = w.in_bytes > w.out_bytes ? w.in_bytes : w.out_bytes;
+        long long chunk = w.count;
+        const bool staged = (min == Mem::Host || mout == Mem::Host);
+        if (staged) {
+            chunk = (long long)(kChunkBytes / per);
+            if (chunk < 1) chunk = 1;
+            if (chunk > w.count) chunk = w.count;
+        }
+        // scratch is shared by the slots; with several chunks in flight the
+        // multi-pass path uses one slot at a time (chunks run in order below)
+        void* scratch = user_scratch;
+        size_t scratch_bytes = user_scratch_bytes;
+        const size_t need = scratch_need(w, chunk);
+        if (need && scratch_bytes < ckg::large_scratch_bytes(w.kind, w.log2n)) {
+            if ((e = grow(&lane->scratch, &lane->scratch_cap, need)) != cudaSuccess) { where = "cudaMalloc(scratch)"; goto done; }
+            scratch = lane->scratch;
+            scratch_bytes = lane->scratch_cap;
+        }
+        const bool serial = need != 0;      // shared scratch: keep chunks on one stream
+        for (long long off = 0, i = 0; off < w.count; off += chunk, ++i) {
+            const long long cnt = (w.count - off < chunk) ? w.count - off : chunk;
+            Slot& sl = lane->slot[serial ? 0 : i % kSlots];
+            const void* din = (const char*)in + (size_t)off * w.in_bytes;
+            void* dout = (char*)out + (size_t)off * w.out_bytes;
+            if (min == Mem::Host) {
+                if (sl.din_cap < (size_t)cnt * w.in_bytes) {
+                    cudaStreamSynchronize(sl.stream);
+                    if ((e = grow(&sl.din, &sl.din_cap, (size_t)chunk * w.in_bytes)) != cudaSuccess) { where = "cudaMalloc(staging)"; goto done; }
+                }
+                if ((e = cudaMemcpyAsync(sl.din, din, (size_t)cnt * w.in_bytes, cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess) { where = "cudaMemcpyAsync(H2D)"; goto done; }
+                din = sl.din;
+            }
+            void* host_out = nullptr;
+            if (mout == Mem::Host) {
+                if (sl.dout_cap < (size_t)cnt * w.out_bytes) {
+                    cudaStreamSynchronize(sl.stream);
+                    if ((e = grow(&sl.dout, &sl.dout_cap, (size_t)chunk * w.out_bytes)) != cudaSuccess) { where = "cudaMalloc(staging)"; goto done; }
+                }
+                host_out = dout;
+                dout = sl.dout;
+            }
+            if ((e = enqueue(c, w, cnt, din, dout, scratch, scratch_bytes, sl.stream)) != cudaSuccess) { where = "kernel launch"; goto done; }
+            if (host_out) {
+                if ((e = cudaMemcpyAsync(host_out, dout, (size_t)cnt * w.out_bytes, cudaMemcpyDeviceToHost, sl.stream)) != cudaSuccess) { where = "cudaMemcpyAsync(D2H)"; goto done; }
+            }
+        }
+    }
+done:
+    for (int i = 0; i < kSlots; ++i) {
+        cudaError_t se = cudaStreamSynchronize(lane->slot[i].stream);
+        if (e == cudaSuccess && se != cudaSuccess) { e = se; where = "cudaStreamSynchronize"; }
+    }
+    if (dep) cudaEventDestroy(dep);
+    release_lane(c, lane);
+    if (e != cudaSuccess) ok = cuda_fail(where, e);
+    return ok;
+}
+
+bool ctx_ok(const CkFftContext* c) { return c && c->magic == kMagic; }
+bool has_fwd(const CkFftContext* c) { return (c->direction & kCkFftDirection_Forward) != 0; }
+bool has_inv(const CkFftContext* c) { return (c->direction & kCkFftDirection_Inverse) != 0; }
+
+// Checks of src/ckfft/ckfft.cpp:38-49 / 80-91 / 99-110 (tmpBuf first for
+// the real inverse, :57-60), then the batch count.
+int check_call(const CkFftContext* c, bool inverse, int n, const void* in, const void* out, long long count)
+{
+    if (!ctx_ok(c) || !(inverse ? has_inv(c) : has_fwd(c)))
+        return fail(ctx_ok(c) ? "context was created without this direction" : "NULL or invalid context");
+    if (!valid_size(n, c->nmax)) return fail("n must be a power of two no larger than the context's nMax");
+    if (!in || !out || in == out) return fail("input and output must be distinct non-NULL buffers");
+    if (count < 0) return fail("count must be >= 0");
+    return 1;
+}
+
+int complex_call(CkFftContext* c, bool inverse, int n, long long count, const CkFftComplex* in,
+                 CkFftComplex* out, void* stream)
+{
+    if (!check_call(c, inverse, n, in, out, count)) return 0;
+    return run(c, make_work(inverse ? ckg::C2C_INV : ckg::C2C_FWD, n, count), in, out, (cudaStream_t)stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+CkFftContext* CkFftInit(int nMax, CkFftDirection direction, void* buf, size_t* bufSize)
+{
+    // src/ckfft/ckfft.cpp:16-31
+    if (nMax <= 0) { set_error("nMax must be > 0"); return nullptr; }
+    if (((unsigned)nMax & ((unsigned)nMax - 1)) != 0) { set_error("nMax must be a power of two"); return nullptr; }
+    if (direction != kCkFftDirection_Forward && direction != kCkFftDirection_Inverse &&
+        direction != kCkFftDirection_Both) {
+        set_error("invalid direction");
+        return nullptr;
+    }
+    if (buf && !bufSize) { set_error("buf given without bufSize"); return nullptr; }
+
+    // src/ckfft/context.cpp:47-72: required size, size query
+    size_t req = sizeof(_CkFftContext);
+    if (req % sizeof(CkFftComplex)) req += sizeof(CkFftComplex) - req % sizeof(CkFftComplex);
+    if (bufSize && (!buf || *bufSize < req)) {
+        *bufSize = req;
+        set_error("buffer size query: %zu bytes required", req);
+        return nullptr;
+    }
+    void* mem = buf ? buf : std::malloc(req);
+    if (!mem) { set_error("out of host memory"); return nullptr; }
+    CkFftContext* c = new (mem) _CkFftContext();
+    c->magic = 0;
+    c->nmax = nMax;
+    c->log2max = log2i(nMax);
+    c->direction = direction;
+    c->own_buf = buf == nullptr;
+    c->dtw = nullptr;
+    c->pool = nullptr;
+
+    cudaError_t e = cudaGetDevice(&c->device);
+    std::vector<float2> tab;
+    if (e != cudaSuccess) { cuda_fail("no CUDA device", e); goto fail_out; }
+    if ((e = ckg::prepare_device()) != cudaSuccess) { cuda_fail("kernel set-up", e); goto fail_out; }
+    ckg::build_twiddles(c->log2max, tab);
+    if ((e = cudaMalloc(&c->dtw, sizeof(float2) * tab.size())) != cudaSuccess) { cuda_fail("cudaMalloc(twiddles)", e); goto fail_out; }
+    if ((e = cudaMemcpy(c->dtw, tab.data(), sizeof(float2) * tab.size(), cudaMemcpyHostToDevice)) != cudaSuccess) { cuda_fail("cudaMemcpy(twiddles)", e); goto fail_out; }
+    c->pool = new (std::nothrow) LanePool();
+    if (!c->pool) { set_error("out of host memory"); goto fail_out; }
+    c->magic = kMagic;
+    return c;
+
+fail_out:
+    if (c->dtw) cudaFree(c->dtw);
+    if (c->own_buf) std::free(mem);
+    return nullptr;
+}
+
+void CkFftShutdown(CkFftContext* c)
+{
+    if (!ctx_ok(c)) return;
+    {
+        DeviceScope scope(c->device);
+        for (Lane* l : c->pool->lanes) free_lane(l);
+        delete c->pool;
+        cudaFree(c->dtw);
+    }
+    c->magic = 0;
+    if (c->own_buf) std::free(c);
+}
+
+int CkFftComplexForward(CkFftContext* c, int n, const CkFftComplex* in, CkFftComplex* out)
+{
+    return complex_call(c, false, n, 1, in, out, nullptr);
+}
+
+int CkFftComplexInverse(CkFftContext* c, int n, const CkFftComplex* in, CkFftComplex* out)
+{
+    return complex_call(c, true, n, 1, in, out, nullptr);
+}
+
+int CkFftRealForward(CkFftContext* c, int n, const float* in, CkFftComplex* out)
+{
+    if (!check_call(c, false, n, in, out, 1)) return 0;
+    return run(c, make_work(ckg::R2C, n, 1), in, out, nullptr);
+}
+
+int CkFftRealInverse(CkFftContext* c, int n, const CkFftComplex* in, float* out, CkFftComplex* tmpBuf)
+{
+    if (!tmpBuf) return fail("tmpBuf must not be NULL");
+    if (!check_call(c, true, n, in, out, 1)) return 0;
+    // tmpBuf (n/2+1 complex) is exactly the multi-pass path's intermediate;
+    // use it when it is device memory on the context's device
+    Work w = make_work(ckg::C2R, n, 1);
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    if (needs_large(w)) {
+        DeviceScope scope(c->device);
+        Mem where;
+        if (scope.ok && classify(tmpBuf, c->device, &where) && where == Mem::Device) {
+            scratch = tmpBuf;
+            scratch_bytes = sizeof(CkFftComplex) * (size_t)(n / 2 + 1);
+        }
+        t_error.clear();
+    }
+    return run(c, w, in, out, nullptr, scratch, scratch_bytes);
+}
+
+const char* CkFftCudaGetLastError(void) { return t_error.c_str(); }
+
+int CkFftCudaComplexForwardBatch(CkFftContext* c, int n, int count, const CkFftComplex* in,
+                                 CkFftComplex* out, void* stream)
+{
+    return complex_call(c, false, n, count, in, out, stream);
+}
+
+int CkFftCudaComplexInverseBatch(CkFftContext* c, int n, int count, const CkFftComplex* in,
+                                 CkFftComplex* out, void* stream)
+{
+    return complex_call(c, true, n, count, in, out, stream);
+}
+
+int CkFftCudaRealForwardBatch(CkFftContext* c, int n, int count, const float* in, CkFftComplex* out,
+                              void* stream)
+{
+    if (!check_call(c, false, n, in, out, count)) return 0;
+    return run(c, make_work(ckg::R2C, n, count), in, out, (cudaStream_t)stream);
+}
+
+int CkFftCudaRealInverseBatch(CkFftContext* c, int n, int count, const CkFftComplex* in, float* out,
+                              void* stream)
+{
+    if (!check_call(c, true, n, in, out, count)) return 0;
+    return run(c, make_work(ckg::C2R, n, count), in, out, (cudaStream_t)stream);
+}
+
+long long CkFftCudaLaunchCount(void) { return ckg::launch_count(); }
+
+}  // extern "C"

@@ -1,0 +1,53 @@
+// dispatch.cu -- routes a launch request to the kernel family for its size.
+#include <atomic>
+#include <mutex>
+#include "kernels.h"
+
+namespace ckg {
+
+cudaError_t launch_small_c2c(bool inv, int log2n, const void* in, void* out, long long count,
+                             long long in_dist, long long out_dist, const float2* tw, cudaStream_t s);
+cudaError_t launch_small_real(bool inv, int log2n, const void* in, void* out, long long count,
+                              long long in_dist, long long out_dist, const float2* tw, cudaStream_t s);
+cudaError_t prepare_small_c2c();
+cudaError_t prepare_small_real();
+cudaError_t prepare_large();
+
+static std::atomic<long long> g_launches{0};
+
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+cudaError_t launch_small(Kind kind, int log2n, const void* in, void* out, long long count,
+                         long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
+{
+    if (count <= 0) return cudaSuccess;
+    cudaError_t e;
+    switch (kind) {
+    case C2C_FWD: e = launch_small_c2c(false, log2n, in, out, count, in_dist, out_dist, tw, s); break;
+    case C2C_INV: e = launch_small_c2c(true, log2n, in, out, count, in_dist, out_dist, tw, s); break;
+    case R2C: e = launch_small_real(false, log2n, in, out, count, in_dist, out_dist, tw, s); break;
+    case C2R: e = launch_small_real(true, log2n, in, out, count, in_dist, out_dist, tw, s); break;
+    default: e = cudaErrorInvalidValue;
+    }
+    if (e == cudaSuccess) count_launch();
+    return e;
+}
+
+cudaError_t prepare_device()
+{
+    static std::mutex mu;
+    static unsigned long long done = 0;     // bit per device ordinal (< 64)
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 64 && (done >> dev) & 1ull) return cudaSuccess;
+    if ((e = prepare_small_c2c()) != cudaSuccess) return e;
+    if ((e = prepare_small_real()) != cudaSuccess) return e;
+    if ((e = prepare_large()) != cudaSuccess) return e;
+    if (dev < 64) done |= 1ull << dev;
+    return cudaSuccess;
+}
+
+}  // namespace ckg

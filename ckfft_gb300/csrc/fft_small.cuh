@@ -1,0 +1,199 @@
+// fft_small.cuh -- single-CTA transforms (complex up to 2^14, real up to 2^15).
+//
+// One kernel launch covers a whole batch.  A CTA holds TPB transforms; each
+// transform is owned by T = N/R threads with R values in registers.  Data is
+// read from HBM once (coalesced over t) and written once, every intermediate
+// stage exchanges through shared memory, and the real-input split / merge
+// steps of the reference (src/ckfft/fft_real_default.cpp:23-62, 79-111) are
+// fused into the kernel's last / first step.
+#pragma once
+#include "fft_core.cuh"
+#include "kernels.h"
+
+namespace ckg {
+
+// Per-size launch shape: R values per thread, TPB transforms per CTA.
+template <int L>
+struct SmallCfg {
+    static constexpr int LOG2R = L < 4 ? L : L < 14 ? 4 : 5;
+    static constexpr int R = 1 << LOG2R;
+    static constexpr int T = (1 << L) / R;
+    static constexpr int TPB = T >= 256 ? 1 : 256 / T;
+    static constexpr int THREADS = T * TPB;
+    static constexpr bool WARP = T <= 32;                  // a transform never spans warps
+    static constexpr int SLOT = padded_len(1 << L);        // shared slots per transform
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)SLOT * TPB;
+};
+
+// ---------------------------------------------------------------- complex
+
+template <int L, bool INV>
+__global__ void __launch_bounds__(SmallCfg<L>::THREADS)
+k_c2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
+            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+{
+    using C = SmallCfg<L>;
+    extern __shared__ float2 smem[];
+    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const long long f = (long long)blockIdx.x * C::TPB + g;
+    const bool live = f < count;
+    float2 v[C::R];
+    if (live) {
+        const float2* src = in + f * in_dist + t;
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) v[m] = __ldcs(src + m * C::T);
+    } else {
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) v[m] = make_float2(0.f, 0.f);
+    }
+    PaddedView view{smem + g * C::SLOT};
+    stockham<L, C::LOG2R, INV, C::WARP>(v, t, tw, view);
+    if (live) {
+        float2* dst = out + f * out_dist + t;
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) __stcs(dst + m * C::T, v[m]);
+    }
+}
+
+// ------------------------------------------------------------ real forward
+// n = 2M reals -> M+1 complex bins (2 * DFT).  LM = log2 M >= 2.
+
+template <int LM>
+__global__ void __launch_bounds__(SmallCfg<LM>::THREADS)
+k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
+            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+{
+    using C = SmallCfg<LM>;
+    constexpr int M = 1 << LM;
+    extern __shared__ float2 smem[];
+    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const long long f = (long long)blockIdx.x * C::TPB + g;
+    const bool live = f < count;
+    float2 v[C::R];
+    if (live) {
+        const float2* src = in + f * in_dist + t;      // packed pairs (x[2p], x[2p+1])
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) v[m] = __ldcs(src + m * C::T);
+    } else {
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) v[m] = make_float2(0.f, 0.f);
+    }
+    PaddedView view{smem + g * C::SLOT};
+    stockham<LM, C::LOG2R, false, C::WARP>(v, t, tw, view);
+    // natural-order half-size spectrum Z to shared memory, then split
+#pragma unroll
+    for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, v[m]);
+    xsync<C::WARP>();
+    const float2* twn = tw + 2 * M;                    // W_n^k, n = 2M
+    if (live) {
+        float2* dst = out + f * out_dist;
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) {
+            const int k = t + m * C::T;
+            const float2 z0 = view.ld(k), z1 = view.ld((M - k) & (M - 1));
+            __stcs(dst + k, real_split(z0, z1, __ldg(twn + k)));
+        }
+        if (t == 0) {
+            const float2 z0 = view.ld(0);
+            __stcs(dst + M, real_split(z0, z0, __ldg(twn + M)));
+        }
+    }
+}
+
+// ------------------------------------------------------------ real inverse
+// M+1 complex bins -> n = 2M reals.
+
+template <int LM>
+__global__ void __launch_bounds__(SmallCfg<LM>::THREADS)
+k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
+            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+{
+    using C = SmallCfg<LM>;
+    constexpr int M = 1 << LM;
+    extern __shared__ float2 smem[];
+    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const long long f = (long long)blockIdx.x * C::TPB + g;
+    const bool live = f < count;
+    PaddedView view{smem + g * C::SLOT};
+    if (live) {
+        const float2* src = in + f * in_dist;
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, __ldcs(src + t + m * C::T));
+        if (t == 0) view.st(M, __ldcs(src + M));
+    } else {
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, make_float2(0.f, 0.f));
+        if (t == 0) view.st(M, make_float2(0.f, 0.f));
+    }
+    xsync<C::WARP>();
+    const float2* twn = tw + 2 * M;
+    float2 v[C::R];
+#pragma unroll
+    for (int m = 0; m < C::R; ++m) {
+        const int p = t + m * C::T;
+        v[m] = real_merge(view.ld(p), view.ld(M - p), __ldg(twn + p));
+    }
+    xsync<C::WARP>();
+    stockham<LM, C::LOG2R, true, C::WARP>(v, t, tw, view);
+    if (live) {
+        float2* dst = out + f * out_dist + t;
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) __stcs(dst + m * C::T, v[m]);
+    }
+}
+
+// ---------------------------------------------------------------- launch
+
+template <class C>
+inline unsigned small_grid(long long count)
+{
+    return (unsigned)((count + C::TPB - 1) / C::TPB);
+}
+
+template <int L, bool INV>
+cudaError_t launch_c2c_L(const void* in, void* out, long long count, long long in_dist,
+                         long long out_dist, const float2* tw, cudaStream_t s)
+{
+    using C = SmallCfg<L>;
+    k_c2c_small<L, INV><<<small_grid<C>(count), C::THREADS, C::SMEM, s>>>(
+        (const float2*)in, (float2*)out, count, in_dist, out_dist, tw);
+    return cudaGetLastError();
+}
+
+template <int LM>
+cudaError_t launch_r2c_L(const void* in, void* out, long long count, long long in_dist,
+                         long long out_dist, const float2* tw, cudaStream_t s)
+{
+    using C = SmallCfg<LM>;
+    k_r2c_small<LM><<<small_grid<C>(count), C::THREADS, C::SMEM, s>>>(
+        (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw);
+    return cudaGetLastError();
+}
+
+template <int LM>
+cudaError_t launch_c2r_L(const void* in, void* out, long long count, long long in_dist,
+                         long long out_dist, const float2* tw, cudaStream_t s)
+{
+    using C = SmallCfg<LM>;
+    k_c2r_small<LM><<<small_grid<C>(count), C::THREADS, C::SMEM, s>>>(
+        (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw);
+    return cudaGetLastError();
+}
+
+template <int L, bool INV>
+cudaError_t attr_c2c_L()
+{
+    return cudaFuncSetAttribute(k_c2c_small<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SmallCfg<L>::SMEM);
+}
+template <int LM>
+cudaError_t attr_real_L()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_r2c_small<LM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SmallCfg<LM>::SMEM);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_c2r_small<LM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SmallCfg<LM>::SMEM);
+}
+
+}  // namespace ckg

@@ -1,0 +1,91 @@
+// fft_small_real.cu -- instantiates the single-CTA real kernels (n = 2^3 .. 2^15)
+// and the closed-form kernel for n = 1, 2, 4.
+#include "fft_small.cuh"
+
+namespace ckg {
+
+cudaError_t launch_small_real(bool inv, int log2n, const void* in, void* out, long long count,
+                              long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
+{
+    // log2n is the real length; kernels are templated on the complex half-length.
+#define CKG_REAL_CASE(LM)                                                                         \
+    case LM + 1:                                                                                  \
+        return inv ? launch_c2r_L<LM>(in, out, count, in_dist, out_dist, tw, s)                   \
+                   : launch_r2c_L<LM>(in, out, count, in_dist, out_dist, tw, s);
+    switch (log2n) {
+        CKG_REAL_CASE(2) CKG_REAL_CASE(3) CKG_REAL_CASE(4) CKG_REAL_CASE(5) CKG_REAL_CASE(6)
+        CKG_REAL_CASE(7) CKG_REAL_CASE(8) CKG_REAL_CASE(9) CKG_REAL_CASE(10) CKG_REAL_CASE(11)
+        CKG_REAL_CASE(12) CKG_REAL_CASE(13) CKG_REAL_CASE(14)
+    default:
+        return cudaErrorInvalidValue;
+    }
+#undef CKG_REAL_CASE
+}
+
+cudaError_t prepare_small_real()
+{
+    cudaError_t e = cudaSuccess;
+#define CKG_ATTR(LM) \
+    if (e == cudaSuccess) e = attr_real_L<LM>();
+    CKG_ATTR(10) CKG_ATTR(11) CKG_ATTR(12) CKG_ATTR(13) CKG_ATTR(14)
+#undef CKG_ATTR
+    return e;
+}
+
+// Closed forms of src/ckfft/fft_real.cpp:20-48 (forward, scaled by 2) and
+// :69-93 (inverse), one frame per thread.  Only the documented n/2+1 output
+// bins are written for the forward n = 4 case.
+__global__ void k_real_tiny(int n, bool inv, const float* __restrict__ in, float* __restrict__ out,
+                            long long count, long long in_dist, long long out_dist)
+{
+    const long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= count) return;
+    if (!inv) {
+        const float* x = in + f * in_dist;          // floats
+        float2* y = (float2*)out + f * out_dist;    // complex
+        if (n == 1) {
+            y[0] = make_float2(x[0] * 2.0f, 0.0f);
+        } else if (n == 2) {
+            y[0] = make_float2((x[0] + x[1]) * 2.0f, 0.0f);
+            y[1] = make_float2((x[0] - x[1]) * 2.0f, 0.0f);
+        } else {
+            const float s02 = (x[0] + x[2]) * 2.0f, d02 = (x[0] - x[2]) * 2.0f;
+            const float s13 = (x[1] + x[3]) * 2.0f, d13 = (x[1] - x[3]) * 2.0f;
+            y[0] = make_float2(s02 + s13, 0.0f);
+            y[1] = make_float2(d02, -d13);
+            y[2] = make_float2(s02 - s13, 0.0f);
+        }
+    } else {
+        const float2* x = (const float2*)in + f * in_dist;   // complex
+        float* y = out + f * out_dist;                       // floats
+        if (n == 1) {
+            y[0] = x[0].x;
+        } else if (n == 2) {
+            y[0] = x[0].x + x[1].x;
+            y[1] = x[0].x - x[1].x;
+        } else {
+            const float s02 = x[0].x + x[2].x;
+            const float s13 = 2.0f * x[1].x;
+            const float d02 = x[0].x - x[2].x;
+            const float d13 = 2.0f * x[1].y;
+            y[0] = s02 + s13;
+            y[1] = d02 - d13;
+            y[2] = s02 - s13;
+            y[3] = d02 + d13;
+        }
+    }
+}
+
+cudaError_t launch_real_tiny(Kind kind, int n, const void* in, void* out, long long count,
+                             long long in_dist, long long out_dist, cudaStream_t s)
+{
+    if (n != 1 && n != 2 && n != 4) return cudaErrorInvalidValue;
+    const int threads = 256;
+    const unsigned blocks = (unsigned)((count + threads - 1) / threads);
+    k_real_tiny<<<blocks, threads, 0, s>>>(n, kind == C2R, (const float*)in, (float*)out, count,
+                                           in_dist, out_dist);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace ckg

@@ -1,0 +1,63 @@
+// kernels.h -- host-side launch interface of the CUDA kernels (internal).
+//
+// Plain C++ (no device code) so that the C-ABI layer can be compiled by the
+// host compiler.  Every launcher enqueues work on `stream` and returns the
+// launch status; none of them synchronises.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+
+namespace ckg {
+
+enum Kind : int { C2C_FWD = 0, C2C_INV = 1, R2C = 2, C2R = 3 };
+
+// Largest log2 size whose whole transform runs in one CTA's shared memory.
+// For R2C/C2R the size is the real length n (the complex half-length is n/2).
+constexpr int kSmallMaxLog2Complex = 14;
+constexpr int kSmallMaxLog2Real = 15;
+
+// Single-CTA transforms of 2^log2n points, `count` of them.
+//   C2C: in/out are complex, dist in complex elements.
+//   R2C: in is float (dist in floats, even), out complex (dist in complex).
+//   C2R: in complex (dist in complex), out float (dist in floats, even).
+// R2C/C2R need log2n >= 3 (n >= 8); smaller real sizes use launch_real_tiny.
+cudaError_t launch_small(Kind kind, int log2n, const void* in, void* out, long long count,
+                         long long in_dist, long long out_dist, const float2* tw, cudaStream_t stream);
+
+// Real transforms of n = 1, 2 or 4 points (closed forms, src/ckfft/fft_real.cpp:20-93).
+cudaError_t launch_real_tiny(Kind kind, int n, const void* in, void* out, long long count,
+                             long long in_dist, long long out_dist, cudaStream_t stream);
+
+// Multi-pass complex transforms for sizes above the single-CTA limit.
+// scratch must hold count_per_group * 2^log2n complex values; the call splits
+// the batch into groups whose scratch fits.  Returns the launch status.
+struct LargePlan {
+    int log2n;       // total size
+    int log2n1;      // column (first-pass) length
+    int log2n2;      // row (second-pass) length
+};
+LargePlan large_plan(int log2n);
+cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out, long long count,
+                             long long in_dist, long long out_dist, const float2* tw,
+                             void* scratch, size_t scratch_bytes, cudaStream_t stream);
+
+// Real transforms above the single-CTA limit: half-size multi-pass complex
+// transform plus a split (forward) or merge (inverse) pass.
+cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long count,
+                             long long in_dist, long long out_dist, const float2* tw,
+                             void* scratch, size_t scratch_bytes, cudaStream_t stream);
+cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long count,
+                             long long in_dist, long long out_dist, const float2* tw,
+                             void* scratch, size_t scratch_bytes, cudaStream_t stream);
+// Scratch bytes one transform of the given kind and size needs on the large path.
+size_t large_scratch_bytes(Kind kind, int log2n);
+
+// Sets per-kernel attributes (dynamic shared memory limits) on the current
+// device.  Idempotent; called when a context is created.
+cudaError_t prepare_device();
+
+// Kernel launches issued so far by this process.
+long long launch_count();
+void count_launch(int n = 1);
+
+}  // namespace ckg

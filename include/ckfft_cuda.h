@@ -1,0 +1,127 @@
+/*
+ * ckfft_cuda.h -- Cricket FFT's C API on a GB300 (sm_103a), plus batched entry points.
+ *
+ * Drop-in: the six CkFft* functions and the three types below have the same
+ * names, signatures, argument meaning, scaling and return codes as the
+ * reference's public header (inc/ckfft/ckfft.h).  A program written against
+ * the reference links unchanged against libckfft_cuda.so.  The header compiles
+ * as C89/C99 as well as C++.
+ *
+ * Pointers given to any entry point may be host memory (pageable or pinned) or
+ * device memory (cudaMalloc / cudaMallocManaged) on the context's device; the
+ * library moves host data through device-resident staging buffers itself.
+ * Every transform runs in hand-written CUDA kernels; there is no CPU path.
+ *
+ * Scaling (identical to the reference): no scaling in either direction; a
+ * complex forward -> inverse round trip multiplies by n; the real forward
+ * output is 2 * DFT(x) over n/2+1 bins, and a real forward -> inverse round
+ * trip multiplies by 2n.
+ */
+#ifndef CKFFT_CUDA_H
+#define CKFFT_CUDA_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Interleaved complex value, 8 bytes.  Replaces inc/ckfft/ckfft.h:10-15. */
+typedef struct
+{
+    float real;
+    float imag;
+}
+CkFftComplex;
+
+/* Opaque context.  Replaces inc/ckfft/ckfft.h:18.  Holds the device-resident
+ * twiddle tables and staging buffers; immutable after CkFftInit apart from a
+ * lock-protected pool of staging lanes, so one context may be used from many
+ * host threads at once (as inc/ckfft/ckfft.h:39-41 promises). */
+typedef struct _CkFftContext CkFftContext;
+
+/* Direction flags.  Replaces inc/ckfft/ckfft.h:21-27. */
+typedef enum
+{
+    kCkFftDirection_Forward = (1 << 0),
+    kCkFftDirection_Inverse = (1 << 1),
+    kCkFftDirection_Both    = (kCkFftDirection_Forward | kCkFftDirection_Inverse)
+}
+CkFftDirection;
+
+/* ----------------------------------------------------------------------
+ * Reference API (same contracts as inc/ckfft/ckfft.h)
+ * ---------------------------------------------------------------------- */
+
+/* Replaces CkFftInit, inc/ckfft/ckfft.h:59 (src/ckfft/ckfft.cpp:14-34,
+ * src/ckfft/context.cpp:45-135).  Returns NULL when nMax <= 0, nMax is not a
+ * power of two, direction is not one of the three flags, buf != NULL with
+ * bufSize == NULL, when *bufSize is given but buf is NULL or *bufSize is too
+ * small (the required size is then written to *bufSize), or when the device
+ * tables cannot be created (no CUDA device, out of device memory).
+ * buf, when given, holds the host-side context object; the twiddle tables
+ * live in device memory owned by the library.  The context is bound to the
+ * CUDA device that is current when CkFftInit is called. */
+CkFftContext* CkFftInit(int nMax, CkFftDirection direction, void* buf, size_t* bufSize);
+
+/* Replaces CkFftRealForward, inc/ckfft/ckfft.h:85 (src/ckfft/ckfft.cpp:36-53).
+ * n real inputs -> n/2+1 complex outputs equal to 2 * DFT(input).
+ * Returns 0 on: NULL or forward-less context, n not a power of two or
+ * n > nMax, NULL input/output, input == output.  Blocks until done. */
+int CkFftRealForward(CkFftContext* context, int n, const float* input, CkFftComplex* output);
+
+/* Replaces CkFftRealInverse, inc/ckfft/ckfft.h:108 (src/ckfft/ckfft.cpp:55-76).
+ * n/2+1 complex inputs -> n real outputs.  tmpBuf (n/2+1 elements) must be
+ * non-NULL, as in the reference (checked first); the kernels keep their
+ * intermediate in on-chip memory and use tmpBuf only when it is device memory
+ * and n needs a multi-pass transform. */
+int CkFftRealInverse(CkFftContext* context, int n, const CkFftComplex* input, float* output, CkFftComplex* tmpBuf);
+
+/* Replaces CkFftComplexForward, inc/ckfft/ckfft.h:129 (src/ckfft/ckfft.cpp:78-95). */
+int CkFftComplexForward(CkFftContext* context, int n, const CkFftComplex* input, CkFftComplex* output);
+
+/* Replaces CkFftComplexInverse, inc/ckfft/ckfft.h:150 (src/ckfft/ckfft.cpp:97-114). */
+int CkFftComplexInverse(CkFftContext* context, int n, const CkFftComplex* input, CkFftComplex* output);
+
+/* Replaces CkFftShutdown, inc/ckfft/ckfft.h:158 (src/ckfft/ckfft.cpp:116-119).
+ * Frees the device tables and staging lanes; frees the context memory only
+ * when CkFftInit allocated it.  CkFftShutdown(NULL) does nothing. */
+void CkFftShutdown(CkFftContext* context);
+
+/* ----------------------------------------------------------------------
+ * Additions (no counterpart in the reference; prefixed CkFftCuda)
+ * ---------------------------------------------------------------------- */
+
+/* Message for the calling thread's most recent failed call ("" if none). */
+const char* CkFftCudaGetLastError(void);
+
+/* Batched transforms: `count` independent transforms of size n stored back to
+ * back (complex: n values per transform; real forward: n floats in, n/2+1
+ * complex out; real inverse: n/2+1 complex in, n floats out).  One kernel
+ * launch covers the whole batch (two or three for multi-pass sizes).
+ *
+ * stream: a cudaStream_t passed as void*.  With NULL the call blocks until
+ * `out` holds the results.  With a stream and device pointers for both `in`
+ * and `out`, the work is only enqueued on that stream (asynchronous).  With a
+ * host pointer on either side the call stages through device buffers,
+ * pipelining copies against compute, and blocks.
+ * Validation and return codes follow the single-transform calls; count == 0
+ * is valid and does nothing; count < 0 returns 0. */
+int CkFftCudaComplexForwardBatch(CkFftContext* context, int n, int count,
+                                 const CkFftComplex* input, CkFftComplex* output, void* stream);
+int CkFftCudaComplexInverseBatch(CkFftContext* context, int n, int count,
+                                 const CkFftComplex* input, CkFftComplex* output, void* stream);
+int CkFftCudaRealForwardBatch(CkFftContext* context, int n, int count,
+                              const float* input, CkFftComplex* output, void* stream);
+int CkFftCudaRealInverseBatch(CkFftContext* context, int n, int count,
+                              const CkFftComplex* input, float* output, void* stream);
+
+/* Number of kernel launches the library has issued in this process (all
+ * contexts, all threads).  Lets a caller count launches inside a timed region. */
+long long CkFftCudaLaunchCount(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* CKFFT_CUDA_H */
