@@ -52,6 +52,7 @@ def parse_args():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-percall", action="store_true")
     return ap.parse_args()
 
 
@@ -309,7 +310,7 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_e2e:
         e2e = measure_e2e(torch, ctx, x, n, frames, bytes_step, world)
 
-    per_call = measure_per_call(torch, ctx, x, n)
+    per_call = None if args.no_percall else measure_per_call(torch, ctx, x, n)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = time_cpu_reference(n, frames)
