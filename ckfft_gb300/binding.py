@@ -74,6 +74,9 @@ def load(path: str | None = None):
 def _declare_extras(lib):
     """Argument types of the later additions to the header, when present."""
     vp, i, ll = C.c_void_p, C.c_int, C.c_longlong
+    if hasattr(lib, "CkFftCudaComplexBatchNoAlloc"):
+        lib.CkFftCudaComplexBatchNoAlloc.restype = i
+        lib.CkFftCudaComplexBatchNoAlloc.argtypes = [vp, i, i, i, vp, vp, vp]
     if hasattr(lib, "CkFftCudaRunJobs"):
         lib.CkFftCudaRunJobs.restype = i
         lib.CkFftCudaRunJobs.argtypes = [vp, vp, i, vp]

@@ -413,6 +413,30 @@ int complex_call(CkFftContext* c, bool inverse, int n, long long count, const Ck
 
 }  // namespace
 
+namespace ckg {
+
+// Read-only view of a context for entry points defined in other files.
+struct ContextView {
+    int nmax;
+    int direction;
+    int device;
+    const float2* tw;
+};
+
+bool context_view(const CkFftContext* c, ContextView* out)
+{
+    if (!ctx_ok(c)) return false;
+    out->nmax = c->nmax;
+    out->direction = c->direction;
+    out->device = c->device;
+    out->tw = c->dtw;
+    return true;
+}
+
+void set_last_error(const char* msg) { set_error("%s", msg); }
+
+}  // namespace ckg
+
 extern "C" {
 
 CkFftContext* CkFftInit(int nMax, CkFftDirection direction, void* buf, size_t* bufSize)

@@ -1,0 +1,134 @@
+// noalloc.cu -- CkFftCudaComplexBatchNoAlloc: complex batches that allocate nothing.
+//
+// Some callers cannot let a library allocate device memory while they run:
+// a real-time audio callback cannot wait for cudaMalloc / cudaFree (both may
+// synchronise the whole device and take unbounded time), a host embedding the
+// library under a fixed memory budget must not see allocations fail or grow
+// mid-stream, and code that owns the device's memory pool (another framework,
+// a custom allocator) does not want a second allocator underneath it.  The
+// regular batch entry points may allocate: staging buffers for host pointers,
+// and the intermediate array of the multi-pass path for n > 2^14.
+//
+// This entry point takes device pointers only and keeps the multi-pass
+// intermediate in one file-scope __device__ array of kNoAllocScratchBytes
+// (8 MiB, 2^20 complex values).  Every GPU that loads the library holds that
+// array until the process exits.  Consequences:
+//   * n is limited to 2^20 (larger sizes are rejected with an error);
+//   * every call on a device shares the one array, so calls whose work
+//     overlaps on that GPU (different streams, or host threads racing) race
+//     on it; callers must order such calls themselves;
+//   * the array keeps the last call's contents; nothing in it has to start
+//     at zero (pass 1 overwrites every element pass 2 reads).
+// The first call on each device looks up the array's device address with
+// cudaGetSymbolAddress while that device is current; that first call should
+// come before any stream capture begins.
+#include <mutex>
+
+#include "ckfft_cuda.h"
+#include "kernels.h"
+
+namespace ckg {
+
+struct ContextView {
+    int nmax;
+    int direction;
+    int device;
+    const float2* tw;
+};
+// Defined in ckfft_api.cpp: validates the handle and copies its fields.
+bool context_view(const CkFftContext* c, ContextView* out);
+void set_last_error(const char* msg);
+
+constexpr int kNoAllocMaxLog2 = 20;
+constexpr size_t kNoAllocScratchBytes = sizeof(float2) << kNoAllocMaxLog2;   // 8 MiB
+
+}  // namespace ckg
+
+// The scratch array.  Host code may not use this name as an address (on the
+// host it denotes a shadow variable); it must go through cudaGetSymbolAddress.
+static __device__ __align__(256) float2 g_noalloc_scratch[1 << ckg::kNoAllocMaxLog2];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (set-up on first use).
+cudaError_t scratch_address(int dev, void** ptr)
+{
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_addr[dev] = p;
+    }
+    *ptr = g_scratch_addr[dev];
+    return cudaSuccess;
+}
+
+int fail(const char* msg)
+{
+    ckg::set_last_error(msg);
+    return 0;
+}
+
+bool on_device(const void* p, int dev)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
+}  // namespace
+
+extern "C" int CkFftCudaComplexBatchNoAlloc(CkFftContext* context, int n, int count, int inverse,
+                                            const CkFftComplex* input, CkFftComplex* output, void* stream)
+{
+    ckg::ContextView cv;
+    if (!ckg::context_view(context, &cv)) return fail("NULL or invalid context");
+    const int need_dir = inverse ? kCkFftDirection_Inverse : kCkFftDirection_Forward;
+    if (!(cv.direction & need_dir)) return fail("context was created without this direction");
+    if (n <= 0 || (n & (n - 1)) != 0 || n > cv.nmax)
+        return fail("n must be a power of two no larger than the context's nMax");
+    if (n > (1 << ckg::kNoAllocMaxLog2))
+        return fail("CkFftCudaComplexBatchNoAlloc: n exceeds 2^20, the size its fixed 8 MiB scratch array holds");
+    if (!input || !output || (const void*)input == (const void*)output)
+        return fail("input and output must be distinct non-NULL buffers");
+    if (count < 0) return fail("count must be >= 0");
+
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return fail("no CUDA device");
+    if (prev != cv.device && cudaSetDevice(cv.device) != cudaSuccess) return fail("cannot select the context's device");
+    int ok = 1;
+    if (!on_device(input, cv.device) || !on_device(output, cv.device)) {
+        ok = fail("CkFftCudaComplexBatchNoAlloc takes device (or managed) memory only; host buffers would need staging allocations");
+    } else if (count > 0) {
+        int log2n = 0;
+        while ((1 << log2n) < n) ++log2n;
+        cudaStream_t s = (cudaStream_t)stream;
+        cudaError_t e;
+        if (log2n <= ckg::kSmallMaxLog2Complex) {
+            e = ckg::launch_small(inverse ? ckg::C2C_INV : ckg::C2C_FWD, log2n, input, output, count, n, n, cv.tw, s);
+        } else {
+            void* scratch = nullptr;
+            e = scratch_address(cv.device, &scratch);
+            if (e == cudaSuccess)
+                e = ckg::launch_large_c2c(inverse != 0, log2n, input, output, count, n, n, cv.tw, scratch,
+                                          ckg::kNoAllocScratchBytes, s);
+        }
+        if (e == cudaSuccess && !stream) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            ckg::set_last_error(cudaGetErrorString(e));
+            ok = 0;
+        }
+    }
+    if (prev >= 0 && prev != cv.device) cudaSetDevice(prev);
+    return ok;
+}

@@ -120,6 +120,23 @@ int CkFftCudaRealInverseBatch(CkFftContext* context, int n, int count,
  * contexts, all threads).  Lets a caller count launches inside a timed region. */
 long long CkFftCudaLaunchCount(void);
 
+/* Complex batch that allocates no memory.  No counterpart in the reference.
+ * For callers that must not allocate while they run: a real-time audio
+ * callback cannot wait for cudaMalloc/cudaFree (they can synchronise the whole
+ * device), and a host with a fixed memory budget or its own device allocator
+ * must not see the library allocate mid-stream.  Same transform and return
+ * codes as CkFftCudaComplex{Forward,Inverse}Batch (inverse != 0 selects the
+ * inverse), but `input` and `output` must be device (or managed) memory, and
+ * n is limited to 2^20: sizes above 2^14 keep their intermediate in one
+ * fixed 8 MiB device array compiled into the library, which every GPU that
+ * loads the library holds until the process exits.  All calls on a device
+ * share that array, so calls that overlap on the GPU race; order them (one
+ * stream, or events).  The first call on a device looks up the array's
+ * address; make that call before any stream capture.  stream == NULL blocks
+ * until done; otherwise the work is enqueued on that cudaStream_t. */
+int CkFftCudaComplexBatchNoAlloc(CkFftContext* context, int n, int count, int inverse,
+                                 const CkFftComplex* input, CkFftComplex* output, void* stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
