@@ -385,6 +385,7 @@ done:
     if (dep) cudaEventDestroy(dep);
     release_lane(c, lane);
     if (e != cudaSuccess) ok = cuda_fail(where, e);
+    else if (ckg::take_device_error()) ok = fail("a kernel's bounded wait for its input copy timed out");
     return ok;
 }
 

@@ -1,5 +1,6 @@
 // dispatch.cu -- routes a launch request to the kernel family for its size.
 #include <atomic>
+#include <cstdlib>
 #include <mutex>
 #include "kernels.h"
 
@@ -30,8 +31,58 @@ cudaError_t launch_small(Kind kind, int log2n, const void* in, void* out, long l
     case C2R: e = launch_small_real(true, log2n, in, out, count, in_dist, out_dist, tw, s); break;
     default: e = cudaErrorInvalidValue;
     }
-    if (e == cudaSuccess) count_launch();
     return e;
+}
+
+int pipe_nbuf()
+{
+    static const int nb = [] {
+        const char* v = std::getenv("CKFFT_CUDA_PIPE_NBUF");
+        if (!v || !*v) return 2;
+        const int x = std::atoi(v);
+        return (x == 0 || x == 2 || x == 3) ? x : 2;
+    }();
+    return nb;
+}
+
+static std::mutex g_err_mu;
+static unsigned* g_err_host[64] = {};
+static unsigned* g_err_dev[64] = {};
+
+unsigned* device_error_word()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    return g_err_dev[dev];
+}
+
+unsigned take_device_error()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || !g_err_host[dev]) return 0;
+    volatile unsigned* h = g_err_host[dev];
+    const unsigned v = *h;
+    if (v) *h = 0;
+    return v;
+}
+
+static cudaError_t prepare_error_word(int dev)
+{
+    std::lock_guard<std::mutex> lock(g_err_mu);
+    if (dev < 0 || dev >= 64 || g_err_host[dev]) return cudaSuccess;
+    void* h = nullptr;
+    void* d = nullptr;
+    cudaError_t e = cudaHostAlloc(&h, 64, cudaHostAllocMapped);
+    if (e != cudaSuccess) return e;
+    e = cudaHostGetDevicePointer(&d, h, 0);
+    if (e != cudaSuccess) {
+        cudaFreeHost(h);
+        return e;
+    }
+    *(volatile unsigned*)h = 0;
+    g_err_host[dev] = (unsigned*)h;
+    g_err_dev[dev] = (unsigned*)d;
+    return cudaSuccess;
 }
 
 cudaError_t prepare_device()
@@ -43,6 +94,7 @@ cudaError_t prepare_device()
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(mu);
     if (dev < 64 && (done >> dev) & 1ull) return cudaSuccess;
+    if ((e = prepare_error_word(dev)) != cudaSuccess) return e;
     if ((e = prepare_small_c2c()) != cudaSuccess) return e;
     if ((e = prepare_small_real()) != cudaSuccess) return e;
     if ((e = prepare_large()) != cudaSuccess) return e;

@@ -224,9 +224,20 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[1 << LOG2R], int t, co
         for (int j = 0; j < RS; ++j) x[j] = v[u + j * U];
         if constexpr (NS > 1) {
             const int k = (t + u * T) & (NS - 1);
-            const float2* lvl = tw + NS * RS;
+            // W^{jk} with W = W_{NS*RS}: the power-of-two multiples W^{2^i k}
+            // are element k of the level NS*RS / 2^i (one coalesced load each);
+            // the rest are products of at most log2(RS) - 1 of those.
+            float2 w[RS];
 #pragma unroll
-            for (int j = 1; j < RS; ++j) x[j] = cmul(x[j], tw_load<INV>(lvl, j * k));
+            for (int p = 1; p < RS; p <<= 1) w[p] = tw_load<INV>(tw + NS * RS / p, k);
+#pragma unroll
+            for (int j = 3; j < RS; ++j) {
+                if ((j & (j - 1)) == 0) continue;
+                const int hb = 1 << (31 - __clz(j));
+                w[j] = cmul(w[hb], w[j - hb]);
+            }
+#pragma unroll
+            for (int j = 1; j < RS; ++j) x[j] = cmul(x[j], w[j]);
         }
         dft<RS, INV>(x);
 #pragma unroll

@@ -20,15 +20,26 @@ struct SmallCfg {
     static constexpr int T = (1 << L) / R;
     static constexpr int TPB = T >= 256 ? 1 : 256 / T;
     static constexpr int THREADS = T * TPB;
+    // resident CTAs asked of ptxas: 64 registers per thread for R <= 16, 128 for R = 32
+    static constexpr int MINB = (R <= 16 ? 1024 : 512) / THREADS > 0 ? (R <= 16 ? 1024 : 512) / THREADS : 1;
     static constexpr bool WARP = T <= 32;                  // a transform never spans warps
     static constexpr int SLOT = padded_len(1 << L);        // shared slots per transform
     static constexpr size_t SMEM = sizeof(float2) * (size_t)SLOT * TPB;
 };
 
+// W_n^(t + m T) for the real split / merge, n = 2 R T: W_n^t * W_{2R}^m, the
+// second factor a compile-time constant when 2R divides 32; else a table load.
+template <int R, int M_, bool INV>
+__device__ __forceinline__ float2 split_twiddle(float2 w_t, const float2* __restrict__ twn, int k)
+{
+    if constexpr (2 * R <= 32) return rot<2 * R, M_, INV>(w_t);
+    else return tw_load<INV>(twn, k);
+}
+
 // ---------------------------------------------------------------- complex
 
 template <int L, bool INV>
-__global__ void __launch_bounds__(SmallCfg<L>::THREADS)
+__global__ void __launch_bounds__(SmallCfg<L>::THREADS, SmallCfg<L>::MINB)
 k_c2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
@@ -59,7 +70,7 @@ k_c2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
 // n = 2M reals -> M+1 complex bins (2 * DFT).  LM = log2 M >= 2.
 
 template <int LM>
-__global__ void __launch_bounds__(SmallCfg<LM>::THREADS)
+__global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
 k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
@@ -87,12 +98,13 @@ k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
     const float2* twn = tw + 2 * M;                    // W_n^k, n = 2M
     if (live) {
         float2* dst = out + f * out_dist;
-#pragma unroll
-        for (int m = 0; m < C::R; ++m) {
+        const float2 w0 = __ldg(twn + t);
+        static_for<0, C::R>([&](auto mc) {
+            constexpr int m = decltype(mc)::value;
             const int k = t + m * C::T;
             const float2 z0 = view.ld(k), z1 = view.ld((M - k) & (M - 1));
-            __stcs(dst + k, real_split(z0, z1, __ldg(twn + k)));
-        }
+            __stcs(dst + k, real_split(z0, z1, split_twiddle<C::R, m, false>(w0, twn, k)));
+        });
         if (t == 0) {
             const float2 z0 = view.ld(0);
             __stcs(dst + M, real_split(z0, z0, __ldg(twn + M)));
@@ -104,7 +116,7 @@ k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
 // M+1 complex bins -> n = 2M reals.
 
 template <int LM>
-__global__ void __launch_bounds__(SmallCfg<LM>::THREADS)
+__global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
 k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
@@ -128,11 +140,12 @@ k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
     xsync<C::WARP>();
     const float2* twn = tw + 2 * M;
     float2 v[C::R];
-#pragma unroll
-    for (int m = 0; m < C::R; ++m) {
+    const float2 w0 = __ldg(twn + t);
+    static_for<0, C::R>([&](auto mc) {
+        constexpr int m = decltype(mc)::value;
         const int p = t + m * C::T;
-        v[m] = real_merge(view.ld(p), view.ld(M - p), __ldg(twn + p));
-    }
+        v[m] = real_merge(view.ld(p), view.ld(M - p), split_twiddle<C::R, m, false>(w0, twn, p));
+    });
     xsync<C::WARP>();
     stockham<LM, C::LOG2R, true, C::WARP>(v, t, tw, view);
     if (live) {

@@ -1,8 +1,34 @@
 // fft_small_real.cu -- instantiates the single-CTA real kernels (n = 2^3 .. 2^15)
 // and the closed-form kernel for n = 1, 2, 4.
-#include "fft_small.cuh"
+#include "fft_pipe.cuh"
 
 namespace ckg {
+
+template <int LM, bool INV>
+static cudaError_t launch_real_any(const void* in, void* out, long long count, long long in_dist,
+                                   long long out_dist, const float2* tw, cudaStream_t s)
+{
+    // in_dist / out_dist in elements of the input / output type (floats on the real side)
+    long long done = 0;
+    cudaError_t e = cudaSuccess;
+    if constexpr (LM >= kPipeMinLog2) {
+        constexpr int K = INV ? C2R : R2C;
+        const long long di = INV ? in_dist : in_dist / 2, dout = INV ? out_dist / 2 : out_dist;
+        const int nb = pipe_nbuf();
+        if (nb == 2) e = launch_pipe<LM, K, 2>(in, out, count, di, dout, tw, device_error_word(), s, &done);
+        else if (nb == 3) e = launch_pipe<LM, K, 3>(in, out, count, di, dout, tw, device_error_word(), s, &done);
+        if (e != cudaSuccess) return e;
+        if (done) count_launch();
+    }
+    if (done < count) {
+        const void* tin = INV ? (const void*)((const float2*)in + done * in_dist) : (const void*)((const float*)in + done * in_dist);
+        void* tout = INV ? (void*)((float*)out + done * out_dist) : (void*)((float2*)out + done * out_dist);
+        e = INV ? launch_c2r_L<LM>(tin, tout, count - done, in_dist, out_dist, tw, s)
+                : launch_r2c_L<LM>(tin, tout, count - done, in_dist, out_dist, tw, s);
+        if (e == cudaSuccess) count_launch();
+    }
+    return e;
+}
 
 cudaError_t launch_small_real(bool inv, int log2n, const void* in, void* out, long long count,
                               long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
@@ -10,8 +36,8 @@ cudaError_t launch_small_real(bool inv, int log2n, const void* in, void* out, lo
     // log2n is the real length; kernels are templated on the complex half-length.
 #define CKG_REAL_CASE(LM)                                                                         \
     case LM + 1:                                                                                  \
-        return inv ? launch_c2r_L<LM>(in, out, count, in_dist, out_dist, tw, s)                   \
-                   : launch_r2c_L<LM>(in, out, count, in_dist, out_dist, tw, s);
+        return inv ? launch_real_any<LM, true>(in, out, count, in_dist, out_dist, tw, s)          \
+                   : launch_real_any<LM, false>(in, out, count, in_dist, out_dist, tw, s);
     switch (log2n) {
         CKG_REAL_CASE(2) CKG_REAL_CASE(3) CKG_REAL_CASE(4) CKG_REAL_CASE(5) CKG_REAL_CASE(6)
         CKG_REAL_CASE(7) CKG_REAL_CASE(8) CKG_REAL_CASE(9) CKG_REAL_CASE(10) CKG_REAL_CASE(11)
@@ -22,12 +48,26 @@ cudaError_t launch_small_real(bool inv, int log2n, const void* in, void* out, lo
 #undef CKG_REAL_CASE
 }
 
+template <int LM>
+static cudaError_t attr_real_all()
+{
+    cudaError_t e = cudaSuccess;
+    if (LM >= 10) e = attr_real_L<LM>();
+    if constexpr (LM >= kPipeMinLog2) {
+        if (e == cudaSuccess) e = attr_pipe<LM, R2C, 2>();
+        if (e == cudaSuccess) e = attr_pipe<LM, C2R, 2>();
+        if (e == cudaSuccess) e = attr_pipe<LM, R2C, 3>();
+        if (e == cudaSuccess) e = attr_pipe<LM, C2R, 3>();
+    }
+    return e;
+}
+
 cudaError_t prepare_small_real()
 {
     cudaError_t e = cudaSuccess;
 #define CKG_ATTR(LM) \
-    if (e == cudaSuccess) e = attr_real_L<LM>();
-    CKG_ATTR(10) CKG_ATTR(11) CKG_ATTR(12) CKG_ATTR(13) CKG_ATTR(14)
+    if (e == cudaSuccess) e = attr_real_all<LM>();
+    CKG_ATTR(6) CKG_ATTR(7) CKG_ATTR(8) CKG_ATTR(9) CKG_ATTR(10) CKG_ATTR(11) CKG_ATTR(12) CKG_ATTR(13) CKG_ATTR(14)
 #undef CKG_ATTR
     return e;
 }

@@ -60,4 +60,14 @@ cudaError_t prepare_device();
 long long launch_count();
 void count_launch(int n = 1);
 
+// Smallest log2 (complex) length served by the pipelined persistent kernels.
+constexpr int kPipeMinLog2 = 6;
+// Buffers per CTA of the pipelined kernels (0 turns them off); from the
+// CKFFT_CUDA_PIPE_NBUF environment variable when set, else the tuned default.
+int pipe_nbuf();
+// Device word (in mapped host memory) where kernels record a timed-out wait,
+// for the current device; take_device_error() reads and clears it.
+unsigned* device_error_word();
+unsigned take_device_error();
+
 }  // namespace ckg

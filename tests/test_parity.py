@@ -188,6 +188,54 @@ def test_large_complex_vs_oracle_and_fp64(torch_cuda, ctx_cache, oracle_mod, l2)
         assert rel_l2(got, oracle_mod.fp64_complex(x, inv)) < 2e-6
 
 
+# ------------------------------------------------- pipelined kernels + tails
+
+def small_tpb(l2):
+    """Frames per CTA group of the single-CTA kernels (SmallCfg in fft_small.cuh)."""
+    r = l2 if l2 < 4 else (4 if l2 < 14 else 5)
+    t = (1 << l2) >> r
+    return 1 if t >= 256 else 256 // t
+
+
+@pytest.mark.parametrize("l2", list(range(6, 15)))
+def test_group_pipeline_with_tail(torch_cuda, ctx_cache, oracle_mod, l2):
+    """3 whole frame groups (bulk-copy pipelined kernel) plus one extra frame (plain kernel)."""
+    n = 1 << l2
+    ctx = ctx_cache(2 * n)
+    o = oracle_mod.Oracle(2 * n)
+    rng = np.random.default_rng(500 + l2)
+    frames = 3 * small_tpb(l2) + 1
+    x = (rng.uniform(-1, 1, (frames, n)) + 1j * rng.uniform(-1, 1, (frames, n))).astype(np.complex64)
+    xr = rng.uniform(-1, 1, (frames, 2 * n)).astype(np.float32)
+    h = (rng.uniform(-1, 1, (frames, n + 1)) + 1j * rng.uniform(-1, 1, (frames, n + 1))).astype(np.complex64)
+    got = {k: run_batch(torch_cuda, ctx, k, n, x) for k in ("cfwd", "cinv")}
+    got["rfwd"] = run_batch(torch_cuda, ctx, "rfwd", 2 * n, xr)
+    got["rinv"] = run_batch(torch_cuda, ctx, "rinv", 2 * n, h)
+    for f in sorted({0, 1, frames // 2, frames - 2, frames - 1}):
+        assert_close(got["cfwd"][f], o.complex(n, x[f], False), n, f"cfwd 2^{l2} frame {f}")
+        assert_close(got["cinv"][f], o.complex(n, x[f], True), n, f"cinv 2^{l2} frame {f}")
+        assert_close(got["rfwd"][f], o.real_forward(2 * n, xr[f]), 2 * n, f"rfwd 2^{l2 + 1} frame {f}")
+        assert_close(got["rinv"][f], o.real_inverse(2 * n, h[f]), 2 * n, f"rinv 2^{l2 + 1} frame {f}")
+
+
+def test_misaligned_input_takes_plain_path(torch_cuda, ctx_cache, oracle_mod):
+    """An input 8 bytes off a 16-byte boundary cannot be bulk-copied; results stay right."""
+    n, frames = 1024, 9
+    ctx = ctx_cache(n)
+    rng = np.random.default_rng(77)
+    x = (rng.uniform(-1, 1, (frames, n)) + 1j * rng.uniform(-1, 1, (frames, n))).astype(np.complex64)
+    buf = torch_cuda.zeros(frames * n + 1, dtype=torch_cuda.complex64, device="cuda")
+    buf[1:] = torch_cuda.from_numpy(x.reshape(-1)).cuda()
+    xin = buf[1:]
+    assert xin.data_ptr() % 16 == 8
+    out = torch_cuda.zeros((frames, n), dtype=torch_cuda.complex64, device="cuda")
+    ctx.check(ctx.batch("cfwd", n, frames, xin, out))
+    got = out.cpu().numpy()
+    o = oracle_mod.Oracle(n)
+    for f in (0, 4, 8):
+        assert_close(got[f], o.complex(n, x[f]), n, f"frame {f}")
+
+
 # ------------------------------------------------------------ memory kinds
 
 @pytest.mark.parametrize("kind,n", [("cfwd", 64), ("cinv", 4096), ("rfwd", 4096), ("rinv", 2048),
