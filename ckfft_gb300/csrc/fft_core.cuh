@@ -176,6 +176,7 @@ __device__ __forceinline__ float2 tw_load(const float2* __restrict__ lvl, int id
 // Padded: one transform per contiguous region, one spare slot every 16
 // elements so that stride-RS butterfly writes fall in distinct 8-byte banks.
 struct PaddedView {
+    static constexpr bool kPadded = true;
     float2* base;
     __device__ __forceinline__ static int pad(int pos) { return pos + (pos >> 4); }
     __device__ __forceinline__ void st(int pos, float2 x) const { base[pad(pos)] = x; }
@@ -191,6 +192,13 @@ struct InterleavedView {
     __device__ __forceinline__ float2 ld(int pos) const { return base[pos * C]; }
 };
 
+template <class View>
+__host__ __device__ constexpr bool is_padded()
+{
+    if constexpr (std::is_same<View, PaddedView>::value) return true;
+    else return false;
+}
+
 // Barrier covering every thread that shares the view (warp or block).
 template <bool WARP>
 __device__ __forceinline__ void xsync()
@@ -201,13 +209,16 @@ __device__ __forceinline__ void xsync()
 
 // ------------------------------------------------------- Stockham engine
 
+// Stage s has radix 2^lrs(s) and span 2^lns(s).  The full radix goes first,
+// where the span is 1 and no twiddles are needed; a smaller remainder radix
+// (log2 N not a multiple of log2 R) is the last stage.
 template <int LOG2N, int LOG2R>
 struct Sched {
     static_assert(LOG2R >= 1 && LOG2R <= LOG2N, "radix must divide the size");
     static constexpr int rem = LOG2N % LOG2R;
     static constexpr int nstages = LOG2N / LOG2R + (rem ? 1 : 0);
-    __host__ __device__ static constexpr int lrs(int s) { return (rem && s == 0) ? rem : LOG2R; }
-    __host__ __device__ static constexpr int lns(int s) { return rem ? (s == 0 ? 0 : rem + (s - 1) * LOG2R) : s * LOG2R; }
+    __host__ __device__ static constexpr int lrs(int s) { return (rem && s == nstages - 1) ? rem : LOG2R; }
+    __host__ __device__ static constexpr int lns(int s) { return s * LOG2R; }
 };
 
 // One radix-RS stage on the R registers of thread t (R/RS butterflies).
@@ -253,16 +264,36 @@ __device__ __forceinline__ void stage_exchange(float2 (&v)[1 << LOG2R], int t, c
     constexpr int R = 1 << LOG2R, RS = 1 << LRS, NS = 1 << LNS;
     constexpr int T = (1 << LOG2N) / R;
     constexpr int U = R / RS;
+    // With the padded layout, positions base + j*NS and t + m*T map to one
+    // base slot plus compile-time offsets when the span is 1 or a multiple of
+    // 16 (writes) and when T is a multiple of 16 (reads).
+    constexpr bool kFastWrite = is_padded<View>() && (NS == 1 || NS % 16 == 0);
+    constexpr bool kFastRead = is_padded<View>() && (T % 16 == 0);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int b = t + u * T;
         const int base = ((b >> LNS) << (LNS + LRS)) + (b & (NS - 1));
+        if constexpr (kFastWrite) {
+            float2* p = view.base + PaddedView::pad(base);
 #pragma unroll
-        for (int j = 0; j < RS; ++j) view.st(base + j * NS, v[u + j * U]);
+            for (int j = 0; j < RS; ++j) {
+                const int off = NS == 1 ? (RS >= 16 ? j + (j >> 4) : j) : j * (NS + NS / 16);
+                p[off] = v[u + j * U];
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < RS; ++j) view.st(base + j * NS, v[u + j * U]);
+        }
     }
     xsync<WARP>();
+    if constexpr (kFastRead) {
+        const float2* q = view.base + PaddedView::pad(t);
 #pragma unroll
-    for (int m = 0; m < R; ++m) v[m] = view.ld(t + m * T);
+        for (int m = 0; m < R; ++m) v[m] = q[m * (T + T / 16)];
+    } else {
+#pragma unroll
+        for (int m = 0; m < R; ++m) v[m] = view.ld(t + m * T);
+    }
     xsync<WARP>();
 }
 

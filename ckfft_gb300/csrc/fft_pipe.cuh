@@ -101,19 +101,7 @@ k_pipe(const float2* __restrict__ in, float2* __restrict__ out, long long ngroup
 #pragma unroll
             for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, v[m]);
             xsync<C::WARP>();
-            const float2* twn = tw + 2 * M;
-            float2* dst = out + f * out_dist;
-            const float2 w0 = __ldg(twn + t);
-            static_for<0, C::R>([&](auto mc) {
-                constexpr int m = decltype(mc)::value;
-                const int k = t + m * C::T;
-                const float2 z0 = view.ld(k), z1 = view.ld((M - k) & (M - 1));
-                __stcs(dst + k, real_split(z0, z1, split_twiddle<C::R, m, false>(w0, twn, k)));
-            });
-            if (t == 0) {
-                const float2 z0 = view.ld(0);
-                __stcs(dst + M, real_split(z0, z0, __ldg(twn + M)));
-            }
+            split_store<C, M>(view, out + f * out_dist, t, tw + 2 * M);
         } else {
             float2* dst = out + f * out_dist + t;
 #pragma unroll

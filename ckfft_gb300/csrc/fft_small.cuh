@@ -36,6 +36,35 @@ __device__ __forceinline__ float2 split_twiddle(float2 w_t, const float2* __rest
     else return tw_load<INV>(twn, k);
 }
 
+// Real forward split of a natural-order half-length spectrum Z held in the
+// view, written as the n/2+1 = M+1 output bins.  Bins k and M-k come from the
+// same pair: with S = z_k + conj z_{M-k}, D = z_k - conj z_{M-k}, P = W_n^k D,
+//   X[k] = S - iP,   X[M-k] = conj(S + iP)
+// (the reference's two per-bin formulas, src/ckfft/fft_real_default.cpp:30-58,
+// share S, D and the twiddle because W_n^{M-k} = -conj W_n^k).  Thread t
+// takes k = t + mT for m < R/2; thread 0 also takes the middle bin k = M/2.
+template <class C, int M, class View>
+__device__ __forceinline__ void split_store(const View& view, float2* __restrict__ dst, int t,
+                                            const float2* __restrict__ twn)
+{
+    const float2 w0 = __ldg(twn + t);
+    static_for<0, C::R / 2>([&](auto mc) {
+        constexpr int m = decltype(mc)::value;
+        const int k = t + m * C::T;
+        const float2 z0 = view.ld(k), z1 = view.ld((M - k) & (M - 1));
+        const float2 w = split_twiddle<C::R, m, false>(w0, twn, k);
+        const float sx = z0.x + z1.x, sy = z0.y - z1.y;
+        const float dx = z0.x - z1.x, dy = z0.y + z1.y;
+        const float px = fmaf(w.x, dx, -w.y * dy), py = fmaf(w.x, dy, w.y * dx);
+        __stcs(dst + k, make_float2(sx + py, sy - px));
+        __stcs(dst + (M - k), make_float2(sx - py, -(sy + px)));
+    });
+    if (t == 0) {
+        const float2 z = view.ld(M / 2);                // X[M/2] = 2 conj Z[M/2]
+        __stcs(dst + M / 2, make_float2(z.x + z.x, -(z.y + z.y)));
+    }
+}
+
 // ---------------------------------------------------------------- complex
 
 template <int L, bool INV>
@@ -95,21 +124,7 @@ k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
 #pragma unroll
     for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, v[m]);
     xsync<C::WARP>();
-    const float2* twn = tw + 2 * M;                    // W_n^k, n = 2M
-    if (live) {
-        float2* dst = out + f * out_dist;
-        const float2 w0 = __ldg(twn + t);
-        static_for<0, C::R>([&](auto mc) {
-            constexpr int m = decltype(mc)::value;
-            const int k = t + m * C::T;
-            const float2 z0 = view.ld(k), z1 = view.ld((M - k) & (M - 1));
-            __stcs(dst + k, real_split(z0, z1, split_twiddle<C::R, m, false>(w0, twn, k)));
-        });
-        if (t == 0) {
-            const float2 z0 = view.ld(0);
-            __stcs(dst + M, real_split(z0, z0, __ldg(twn + M)));
-        }
-    }
+    if (live) split_store<C, M>(view, out + f * out_dist, t, tw + 2 * M);
 }
 
 // ------------------------------------------------------------ real inverse
@@ -127,26 +142,27 @@ k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
     const long long f = (long long)blockIdx.x * C::TPB + g;
     const bool live = f < count;
     PaddedView view{smem + g * C::SLOT};
-    if (live) {
-        const float2* src = in + f * in_dist;
-#pragma unroll
-        for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, __ldcs(src + t + m * C::T));
-        if (t == 0) view.st(M, __ldcs(src + M));
-    } else {
-#pragma unroll
-        for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, make_float2(0.f, 0.f));
-        if (t == 0) view.st(M, make_float2(0.f, 0.f));
-    }
-    xsync<C::WARP>();
     const float2* twn = tw + 2 * M;
     float2 v[C::R];
-    const float2 w0 = __ldg(twn + t);
-    static_for<0, C::R>([&](auto mc) {
-        constexpr int m = decltype(mc)::value;
-        const int p = t + m * C::T;
-        v[m] = real_merge(view.ld(p), view.ld(M - p), split_twiddle<C::R, m, false>(w0, twn, p));
-    });
-    xsync<C::WARP>();
+    if (live) {
+        // both merge operands straight from HBM: X[p] coalesced ascending and
+        // X[M-p] coalesced descending (the second read of each line hits cache)
+        const float2* src = in + f * in_dist;
+        float2 a[C::R], b[C::R];
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) {
+            a[m] = __ldg(src + t + m * C::T);
+            b[m] = __ldg(src + (M - t - m * C::T));
+        }
+        const float2 w0 = __ldg(twn + t);
+        static_for<0, C::R>([&](auto mc) {
+            constexpr int m = decltype(mc)::value;
+            v[m] = real_merge(a[m], b[m], split_twiddle<C::R, m, false>(w0, twn, t + m * C::T));
+        });
+    } else {
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) v[m] = make_float2(0.f, 0.f);
+    }
     stockham<LM, C::LOG2R, true, C::WARP>(v, t, tw, view);
     if (live) {
         float2* dst = out + f * out_dist + t;
