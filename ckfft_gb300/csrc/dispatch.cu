@@ -3,6 +3,7 @@
 #include <cstdlib>
 #include <mutex>
 #include "kernels.h"
+#include "tuning_table.h"
 
 namespace ckg {
 
@@ -34,15 +35,17 @@ cudaError_t launch_small(Kind kind, int log2n, const void* in, void* out, long l
     return e;
 }
 
-int pipe_nbuf()
+int variant_for(Kind kind, int log2c)
 {
-    static const int nb = [] {
+    static const int forced = [] {
         const char* v = std::getenv("CKFFT_CUDA_PIPE_NBUF");
-        if (!v || !*v) return 2;
+        if (!v || !*v) return -1;
         const int x = std::atoi(v);
-        return (x == 0 || x == 2 || x == 3) ? x : 2;
+        return (x == 0 || x == 2 || x == 3) ? x : -1;
     }();
-    return nb;
+    if (forced >= 0) return forced;
+    if (kind < 0 || kind > 3 || log2c < 0 || log2c > 14) return 0;
+    return kTunedVariant[kind][log2c];
 }
 
 static std::mutex g_err_mu;

@@ -13,7 +13,7 @@ static cudaError_t launch_c2c_any(const void* in, void* out, long long count, lo
     cudaError_t e = cudaSuccess;
     if constexpr (L >= kPipeMinLog2) {
         constexpr int K = INV ? C2C_INV : C2C_FWD;
-        const int nb = pipe_nbuf();
+        const int nb = variant_for((Kind)K, L);
         if (nb == 2) e = launch_pipe<L, K, 2>(in, out, count, in_dist, out_dist, tw, device_error_word(), s, &done);
         else if (nb == 3) e = launch_pipe<L, K, 3>(in, out, count, in_dist, out_dist, tw, device_error_word(), s, &done);
         if (e != cudaSuccess) return e;

@@ -14,7 +14,7 @@ static cudaError_t launch_real_any(const void* in, void* out, long long count, l
     if constexpr (LM >= kPipeMinLog2) {
         constexpr int K = INV ? C2R : R2C;
         const long long di = INV ? in_dist : in_dist / 2, dout = INV ? out_dist / 2 : out_dist;
-        const int nb = pipe_nbuf();
+        const int nb = variant_for((Kind)K, LM);
         if (nb == 2) e = launch_pipe<LM, K, 2>(in, out, count, di, dout, tw, device_error_word(), s, &done);
         else if (nb == 3) e = launch_pipe<LM, K, 3>(in, out, count, di, dout, tw, device_error_word(), s, &done);
         if (e != cudaSuccess) return e;

@@ -62,9 +62,11 @@ void count_launch(int n = 1);
 
 // Smallest log2 (complex) length served by the pipelined persistent kernels.
 constexpr int kPipeMinLog2 = 6;
-// Buffers per CTA of the pipelined kernels (0 turns them off); from the
-// CKFFT_CUDA_PIPE_NBUF environment variable when set, else the tuned default.
-int pipe_nbuf();
+// Kernel variant for a single-CTA size: 0 plain, 2 / 3 pipelined with that
+// many bulk-copy buffers.  From the committed autotune table (tuning_table.h)
+// unless the CKFFT_CUDA_PIPE_NBUF environment variable forces one variant
+// (the autotuner uses it to measure each variant).
+int variant_for(Kind kind, int log2c);
 // Device word (in mapped host memory) where kernels record a timed-out wait,
 // for the current device; take_device_error() reads and clears it.
 unsigned* device_error_word();
