@@ -80,6 +80,32 @@ def _declare_extras(lib):
     if hasattr(lib, "CkFftCudaRunJobs"):
         lib.CkFftCudaRunJobs.restype = i
         lib.CkFftCudaRunJobs.argtypes = [vp, vp, i, vp]
+        lib.CkFftCudaPlanJobs.restype = vp
+        lib.CkFftCudaPlanJobs.argtypes = [vp, vp, i]
+        lib.CkFftCudaExecPlan.restype = i
+        lib.CkFftCudaExecPlan.argtypes = [vp, vp]
+        lib.CkFftCudaDestroyPlan.restype = None
+        lib.CkFftCudaDestroyPlan.argtypes = [vp]
+        lib.CkFftCudaPlanBytes.restype = ll
+        lib.CkFftCudaPlanBytes.argtypes = [vp]
+
+
+class Job(C.Structure):
+    """CkFftCudaJob: `count` transforms of size n between device buffers."""
+    _fields_ = [("kind", C.c_int), ("n", C.c_int), ("count", C.c_int),
+                ("input", C.c_void_p), ("output", C.c_void_p)]
+
+
+KIND = {"cfwd": 0, "cinv": 1, "rfwd": 2, "rinv": 3}
+
+
+def job_array(jobs):
+    """jobs: iterable of (kind, n, count, input, output) with kind a KIND key or int."""
+    jobs = list(jobs)
+    arr = (Job * max(1, len(jobs)))()
+    for i, (kind, n, count, inp, out) in enumerate(jobs):
+        arr[i] = Job(KIND.get(kind, kind), n, count, ptr(inp), ptr(out))
+    return arr, len(jobs)
 
 
 def last_error() -> str:
@@ -155,6 +181,41 @@ class Context:
         s = getattr(stream, "cuda_stream", stream)
         return fn(self.handle, n, count, ptr(inp), ptr(out), s)
 
+    def run_jobs(self, jobs, stream=None) -> int:
+        arr, n = job_array(jobs)
+        s = getattr(stream, "cuda_stream", stream)
+        return self.lib.CkFftCudaRunJobs(self.handle, C.cast(arr, C.c_void_p), n, s)
+
+    def plan(self, jobs) -> "Plan":
+        return Plan(self, jobs)
+
     def check(self, rc: int, what: str = "call"):
         if rc != 1:
             raise CkFftError(f"{what} failed: {last_error()}")
+
+
+class Plan:
+    """CkFftCudaPlan: a mixed run captured once, replayed with one graph launch."""
+
+    def __init__(self, ctx: Context, jobs):
+        self.lib = ctx.lib
+        arr, n = job_array(jobs)
+        self.handle = self.lib.CkFftCudaPlanJobs(ctx.handle, C.cast(arr, C.c_void_p), n)
+        if not self.handle:
+            raise CkFftError(f"CkFftCudaPlanJobs failed: {last_error()}")
+        self.bytes = self.lib.CkFftCudaPlanBytes(self.handle)
+
+    def exec(self, stream=None) -> int:
+        s = getattr(stream, "cuda_stream", stream)
+        return self.lib.CkFftCudaExecPlan(self.handle, s)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.CkFftCudaDestroyPlan(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -14,6 +14,7 @@ cudaError_t launch_small_real(bool inv, int log2n, const void* in, void* out, lo
 cudaError_t prepare_small_c2c();
 cudaError_t prepare_small_real();
 cudaError_t prepare_large();
+cudaError_t prepare_jobs();
 
 static std::atomic<long long> g_launches{0};
 
@@ -101,6 +102,7 @@ cudaError_t prepare_device()
     if ((e = prepare_small_c2c()) != cudaSuccess) return e;
     if ((e = prepare_small_real()) != cudaSuccess) return e;
     if ((e = prepare_large()) != cudaSuccess) return e;
+    if ((e = prepare_jobs()) != cudaSuccess) return e;
     if (dev < 64) done |= 1ull << dev;
     return cudaSuccess;
 }

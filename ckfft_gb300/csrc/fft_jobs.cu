@@ -1,0 +1,279 @@
+// fft_jobs.cu -- the persistent job kernel: a mixed run of transforms (sizes,
+// kinds and directions all different) in one launch fed by a device queue.
+//
+// Every CTA stays resident and repeatedly takes the next unit (jobs.h) with
+// one atomic add on the queue head, then runs the device function for that
+// unit's operation and size:
+//   * single-CTA units run the same frame bodies as the batched kernels
+//     (fft_small.cuh), each group of T threads on its own frame pointer;
+//   * column / row / split / merge units run the multi-pass bodies
+//     (fft_passes.cuh) with L2-only loads, because their inputs were written
+//     by other CTAs earlier in this launch (L1 is not coherent across SMs).
+// A phase unit first waits (bounded, thread 0, acquire load) for its
+// transform's counter to reach `need`; when a unit of a transform finishes,
+// thread 0 fences and adds one to the counter (release).  A wait that runs
+// out records an error in the error word and the unit is skipped.
+#include "fft_passes.cuh"
+#include "fft_small.cuh"
+#include "jobs.h"
+#include "kernels.h"
+#include "tma.cuh"
+
+namespace ckg {
+
+constexpr unsigned kErrCounterTimeout = 2u;
+
+__device__ __forceinline__ bool wait_counter(const int* p, int need, unsigned* err)
+{
+#pragma unroll 1
+    for (int it = 0; it < (1 << 26); ++it) {
+        int v;
+        asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+        if (v >= need) return true;
+        __nanosleep(64);
+    }
+    if (err) *(volatile unsigned*)err = kErrCounterTimeout;
+    return false;
+}
+
+// ----------------------------------------------------------- unit bodies
+
+template <int OP, int L>
+__device__ __noinline__ void run_single(const Unit& u, const JobsArgs& a, float2* smem)
+{
+    using C = SmallCfg<L>;
+    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const bool live = g < u.count;
+    FrameDesc fd{nullptr, nullptr};
+    if (live) fd = a.frames[u.first + g];
+    const PaddedView view{smem + g * C::SLOT};
+    if constexpr (OP == U_C2C_FWD) frame_c2c<L, false>(fd.in, fd.out, live, t, view, a.tw);
+    else if constexpr (OP == U_C2C_INV) frame_c2c<L, true>(fd.in, fd.out, live, t, view, a.tw);
+    else if constexpr (OP == U_R2C) frame_r2c<L>(fd.in, fd.out, live, t, view, a.tw);
+    else frame_c2r<L>(fd.in, fd.out, live, t, view, a.tw);
+}
+
+// Real n = 1, 2, 4 closed forms (src/ckfft/fft_real.cpp:20-93), one frame per thread.
+__device__ __noinline__ void run_rtiny(const Unit& u, const JobsArgs& a, bool inv)
+{
+    const int g = threadIdx.x;
+    if (g >= u.count) return;
+    const FrameDesc fd = a.frames[u.first + g];
+    const int n = 1 << u.log2a;
+    if (!inv) {
+        const float* x = (const float*)fd.in;
+        float2* y = fd.out;
+        if (n == 1) {
+            y[0] = make_float2(x[0] * 2.0f, 0.0f);
+        } else if (n == 2) {
+            y[0] = make_float2((x[0] + x[1]) * 2.0f, 0.0f);
+            y[1] = make_float2((x[0] - x[1]) * 2.0f, 0.0f);
+        } else {
+            const float s02 = (x[0] + x[2]) * 2.0f, d02 = (x[0] - x[2]) * 2.0f;
+            const float s13 = (x[1] + x[3]) * 2.0f, d13 = (x[1] - x[3]) * 2.0f;
+            y[0] = make_float2(s02 + s13, 0.0f);
+            y[1] = make_float2(d02, -d13);
+            y[2] = make_float2(s02 - s13, 0.0f);
+        }
+    } else {
+        const float2* x = fd.in;
+        float* y = (float*)fd.out;
+        if (n == 1) {
+            y[0] = x[0].x;
+        } else if (n == 2) {
+            y[0] = x[0].x + x[1].x;
+            y[1] = x[0].x - x[1].x;
+        } else {
+            const float s02 = x[0].x + x[2].x, s13 = 2.0f * x[1].x;
+            const float d02 = x[0].x - x[2].x, d13 = 2.0f * x[1].y;
+            y[0] = s02 + s13;
+            y[1] = d02 - d13;
+            y[2] = s02 - s13;
+            y[3] = d02 + d13;
+        }
+    }
+}
+
+__device__ __forceinline__ float2* pick(const LargeDesc& d, int sel)
+{
+    return sel == B_IN ? const_cast<float2*>(d.in) : sel == B_OUT ? d.out : d.scratch;
+}
+
+// A pass unit carries kJobThreads / THREADS whole tiles, one per subgroup.
+template <int OP, int LS>
+__device__ __noinline__ void run_pass(const Unit& u, const JobsArgs& a, float2* smem)
+{
+    using P = PassCfg<LS>;
+    const int s = threadIdx.x / P::THREADS, tid = threadIdx.x % P::THREADS;
+    const LargeDesc d = a.large[u.job];
+    const float2* src = pick(d, u.sel & 15);
+    float2* dst = pick(d, u.sel >> 4);
+    float2* my = smem + s * P::SLOTS;
+    const long long tile = (long long)u.first + s;
+    if constexpr (OP == U_COLS_FWD) pass_cols<LS, false, true>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_COLS_INV) pass_cols<LS, true, true>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_ROWS_FWD) pass_rows<LS, false, true>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else pass_rows<LS, true, true>(src, dst, u.log2b, tile, tid, my, a.tw);
+}
+
+__device__ __noinline__ void run_split_merge(const Unit& u, const JobsArgs& a)
+{
+    const LargeDesc d = a.large[u.job];
+    const long long M = 1ll << u.log2a;
+    const float2* twn = a.tw + 2 * M;
+    const float2* src = pick(d, u.sel & 15);
+    float2* dst = pick(d, u.sel >> 4);
+    for (long long e = u.first + (long long)threadIdx.x; e < (long long)u.first + u.count; e += kJobThreads) {
+        if (u.op == U_SPLIT) split_pair_inplace<true>(dst, M, e, twn);
+        else merge_elem<true>(src, dst, M, e, twn);
+    }
+}
+
+// ---------------------------------------------------------------- dispatch
+
+#define CKG_SINGLE_CASES(OP)                                                          \
+    switch (u.log2a) {                                                                \
+    case 0: if constexpr (OP <= U_C2C_INV) run_single<OP, 0>(u, a, smem); break;      \
+    case 1: if constexpr (OP <= U_C2C_INV) run_single<OP, 1>(u, a, smem); break;      \
+    case 2: run_single<OP, 2>(u, a, smem); break;                                     \
+    case 3: run_single<OP, 3>(u, a, smem); break;                                     \
+    case 4: run_single<OP, 4>(u, a, smem); break;                                     \
+    case 5: run_single<OP, 5>(u, a, smem); break;                                     \
+    case 6: run_single<OP, 6>(u, a, smem); break;                                     \
+    case 7: run_single<OP, 7>(u, a, smem); break;                                     \
+    case 8: run_single<OP, 8>(u, a, smem); break;                                     \
+    case 9: run_single<OP, 9>(u, a, smem); break;                                     \
+    case 10: run_single<OP, 10>(u, a, smem); break;                                   \
+    case 11: run_single<OP, 11>(u, a, smem); break;                                   \
+    case 12: run_single<OP, 12>(u, a, smem); break;                                   \
+    case 13: run_single<OP, 13>(u, a, smem); break;                                   \
+    default: break;                                                                   \
+    }
+
+#define CKG_PASS_CASES(OP)                                                            \
+    switch (u.log2a) {                                                                \
+    case 7: run_pass<OP, 7>(u, a, smem); break;                                       \
+    case 8: run_pass<OP, 8>(u, a, smem); break;                                       \
+    case 9: run_pass<OP, 9>(u, a, smem); break;                                       \
+    case 10: run_pass<OP, 10>(u, a, smem); break;                                     \
+    default: break;                                                                   \
+    }
+
+template <int OP>
+__device__ __forceinline__ void single_switch(const Unit& u, const JobsArgs& a, float2* smem)
+{
+    CKG_SINGLE_CASES(OP)
+}
+
+template <int OP>
+__device__ __forceinline__ void pass_switch(const Unit& u, const JobsArgs& a, float2* smem)
+{
+    CKG_PASS_CASES(OP)
+}
+
+__device__ __forceinline__ void dispatch(const Unit& u, const JobsArgs& a, float2* smem)
+{
+    switch (u.op) {
+    case U_C2C_FWD: single_switch<U_C2C_FWD>(u, a, smem); break;
+    case U_C2C_INV: single_switch<U_C2C_INV>(u, a, smem); break;
+    case U_R2C: single_switch<U_R2C>(u, a, smem); break;
+    case U_C2R: single_switch<U_C2R>(u, a, smem); break;
+    case U_RTINY_FWD: run_rtiny(u, a, false); break;
+    case U_RTINY_INV: run_rtiny(u, a, true); break;
+    case U_COLS_FWD: pass_switch<U_COLS_FWD>(u, a, smem); break;
+    case U_COLS_INV: pass_switch<U_COLS_INV>(u, a, smem); break;
+    case U_ROWS_FWD: pass_switch<U_ROWS_FWD>(u, a, smem); break;
+    case U_ROWS_INV: pass_switch<U_ROWS_INV>(u, a, smem); break;
+    case U_SPLIT:
+    case U_MERGE: run_split_merge(u, a); break;
+    default: break;
+    }
+}
+
+__global__ void __launch_bounds__(kJobThreads, 2) k_jobs(JobsArgs a)
+{
+    extern __shared__ __align__(128) float2 smem[];
+    __shared__ int s_unit;
+    __shared__ int s_ok;
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = atomicAdd(a.head, 1);
+        __syncthreads();
+        const int ui = s_unit;
+        if (ui >= a.nunits) break;
+        const Unit u = a.units[ui];
+        if (threadIdx.x == 0) s_ok = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err) : 1;
+        __syncthreads();
+        if (s_ok) dispatch(u, a, smem);
+        __syncthreads();
+        if (u.job >= 0 && threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(a.done + u.job, 1);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host
+
+template <int L>
+constexpr size_t single_smem()
+{
+    return sizeof(float2) * (size_t)SmallCfg<L>::SLOT * (kJobThreads / SmallCfg<L>::T);
+}
+template <int LS>
+constexpr size_t pass_smem()
+{
+    return PassCfg<LS>::SMEM * (kJobThreads / PassCfg<LS>::THREADS);
+}
+constexpr size_t cmax(size_t a, size_t b) { return a > b ? a : b; }
+
+size_t jobs_smem_bytes()
+{
+    size_t m = 0;
+    m = cmax(m, single_smem<2>()); m = cmax(m, single_smem<3>()); m = cmax(m, single_smem<4>());
+    m = cmax(m, single_smem<5>()); m = cmax(m, single_smem<6>()); m = cmax(m, single_smem<7>());
+    m = cmax(m, single_smem<8>()); m = cmax(m, single_smem<9>()); m = cmax(m, single_smem<10>());
+    m = cmax(m, single_smem<11>()); m = cmax(m, single_smem<12>()); m = cmax(m, single_smem<13>());
+    m = cmax(m, pass_smem<7>()); m = cmax(m, pass_smem<8>()); m = cmax(m, pass_smem<9>());
+    m = cmax(m, pass_smem<10>());
+    return (m + 127) / 128 * 128;
+}
+
+int jobs_grid();
+
+cudaError_t prepare_jobs()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jobs_smem_bytes());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_jobs, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    jobs_grid();
+    return cudaSuccess;
+}
+
+// Resident CTAs of the job kernel on the current device (cached per device;
+// safe to call during stream capture once cached).
+int jobs_grid()
+{
+    static int cache[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && cache[dev]) return cache[dev];
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_jobs, kJobThreads, jobs_smem_bytes()) != cudaSuccess || per < 1)
+        per = 1;
+    const int g = per * (sms > 0 ? sms : 1);
+    if (dev >= 0 && dev < 64) cache[dev] = g;
+    return g;
+}
+
+// Enqueues the job kernel (the caller counts the launch).
+cudaError_t launch_jobs(const JobsArgs& a, cudaStream_t s)
+{
+    if (a.nunits <= 0) return cudaSuccess;
+    const int grid = jobs_grid();
+    k_jobs<<<grid < a.nunits ? grid : a.nunits, kJobThreads, jobs_smem_bytes(), s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace ckg

@@ -13,52 +13,12 @@
 // rows (pass 2) per CTA so every warp access covers C*8 contiguous bytes.
 // Real sizes run the half-length complex transform plus a split (forward) or
 // merge (inverse) pass, the algebra of src/ckfft/fft_real_default.cpp.
-#include "fft_core.cuh"
+#include "fft_passes.cuh"
 #include "kernels.h"
 
 namespace ckg {
 
-// Shape of a sub-transform of 2^LS points inside a pass: R values per thread,
-// C sequences per CTA.
-template <int LS>
-struct PassCfg {
-    static constexpr int LOG2R = LS < 4 ? LS : LS <= 10 ? 4 : 5;
-    static constexpr int R = 1 << LOG2R;
-    static constexpr int T = (1 << LS) / R;
-    // at most 512 threads (so up to 128 registers) and ~140 KB of shared memory
-    static constexpr int C = 512 / T < 16 ? 512 / T : 16;
-    static constexpr int THREADS = C * T;
-    // interleaved (pass 1 and pass-2 transpose) and per-row padded (pass 2) layouts
-    static constexpr int INTERLEAVED = (1 << LS) * C + ((1 << LS) * C >> 4) + 1;
-    static constexpr int BLOCKED = C * padded_len(1 << LS);
-    static constexpr size_t SMEM = sizeof(float2) * (size_t)(INTERLEAVED > BLOCKED ? INTERLEAVED : BLOCKED);
-};
-
-// Element pos of sequence c in an interleaved tile, padded every 16 slots.
-template <int C>
-struct TileView {
-    float2* base;
-    int c;
-    __device__ __forceinline__ static int slot(int pos, int c) { const int p = pos * C + c; return p + (p >> 4); }
-    __device__ __forceinline__ void st(int pos, float2 x) const { base[slot(pos, c)] = x; }
-    __device__ __forceinline__ float2 ld(int pos) const { return base[slot(pos, c)]; }
-};
-
-// W_N^p for 0 <= p < N = 2^ln from two short table levels:
-// W_N^p = W_{N/2^s}^(p >> s) * W_N^(p mod 2^s), s = ceil(ln/2).
-// Sizes on this path are at most 2^28, so p fits in 32 bits.
-template <bool INV>
-__device__ __forceinline__ float2 big_twiddle(const float2* __restrict__ tw, int ln, int p)
-{
-    const int s = (ln + 1) >> 1;
-    const int hi = p >> s, lo = p & ((1 << s) - 1);
-    const float2 a = __ldg(tw + (1 << (ln - s)) + hi);
-    const float2 b = __ldg(tw + (1 << ln) + lo);
-    const float2 w = cmul(a, b);
-    return INV ? conjf2(w) : w;
-}
-
-// ------------------------------------------------------------ pass 1
+// ------------------------------------------------------------ pass kernels
 
 template <int LA, bool INV>
 __global__ void __launch_bounds__(PassCfg<LA>::THREADS)
@@ -67,31 +27,10 @@ k_cols(const float2* __restrict__ in, float2* __restrict__ out, long long count,
 {
     using P = PassCfg<LA>;
     extern __shared__ float2 smem[];
-    const int c = threadIdx.x % P::C, t = threadIdx.x / P::C;
-    const long long n2len = 1ll << log2n2;
-    const long long tiles = n2len / P::C;
+    const long long tiles = (1ll << log2n2) / P::C;
     const long long f = blockIdx.x / tiles;
-    const long long n2 = (blockIdx.x % tiles) * P::C + c;
-    const float2* src = in + f * in_dist + n2;
-    float2 v[P::R];
-#pragma unroll
-    for (int m = 0; m < P::R; ++m) v[m] = __ldcs(src + (long long)(t + m * P::T) * n2len);
-    TileView<P::C> view{smem, c};
-    stockham<LA, P::LOG2R, INV, false>(v, t, tw, view);
-    const int ln = LA + log2n2;
-    float2* dst = out + f * out_dist + n2 + (long long)t * n2len;
-    const long long step = (long long)P::T * n2len;
-#pragma unroll
-    for (int m = 0; m < P::R; ++m) {
-        const int k1 = t + m * P::T;
-        __stcs(dst + m * step, cmul(v[m], big_twiddle<INV>(tw, ln, (int)n2 * k1)));
-        // keep the compiler from hoisting every twiddle load ahead of the
-        // stores (that would need 4 more registers per value)
-        if ((m & 3) == 3) asm volatile("" ::: "memory");
-    }
+    pass_cols<LA, INV, false>(in + f * in_dist, out + f * out_dist, log2n2, blockIdx.x % tiles, threadIdx.x, smem, tw);
 }
-
-// ------------------------------------------------------------ pass 2
 
 template <int LB, bool INV>
 __global__ void __launch_bounds__(PassCfg<LB>::THREADS)
@@ -99,31 +38,10 @@ k_rows(const float2* __restrict__ in, float2* __restrict__ out, long long count,
        long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
     using P = PassCfg<LB>;
-    constexpr int N2 = 1 << LB;
     extern __shared__ float2 smem[];
-    const int r = threadIdx.x / P::T, t = threadIdx.x % P::T;
-    const long long n1len = 1ll << log2n1;
-    const long long tiles = n1len / P::C;
+    const long long tiles = (1ll << log2n1) / P::C;
     const long long f = blockIdx.x / tiles;
-    const long long row0 = (blockIdx.x % tiles) * P::C;
-    const float2* src = in + f * in_dist + (row0 + r) * N2 + t;
-    float2 v[P::R];
-#pragma unroll
-    for (int m = 0; m < P::R; ++m) v[m] = __ldcs(src + m * P::T);
-    PaddedView view{smem + r * padded_len(N2)};
-    stockham<LB, P::LOG2R, INV, (P::T <= 32)>(v, t, tw, view);
-    __syncthreads();
-    // transpose through shared memory so that stores run along rows k1
-#pragma unroll
-    for (int m = 0; m < P::R; ++m) smem[TileView<P::C>::slot(t + m * P::T, r)] = v[m];
-    __syncthreads();
-    const int r2 = threadIdx.x % P::C, t2 = threadIdx.x / P::C;
-    float2* dst = out + f * out_dist + row0 + r2;
-#pragma unroll
-    for (int m = 0; m < P::R; ++m) {
-        const int k2 = t2 + m * P::T;
-        __stcs(dst + (long long)k2 * n1len, smem[TileView<P::C>::slot(k2, r2)]);
-    }
+    pass_rows<LB, INV, false>(in + f * in_dist, out + f * out_dist, log2n1, blockIdx.x % tiles, threadIdx.x, smem, tw);
 }
 
 // ------------------------------------------------- real split / merge passes
@@ -134,25 +52,11 @@ __global__ void k_split_inplace(float2* __restrict__ z, long long count, int lm,
                                 const float2* __restrict__ tw)
 {
     const long long M = 1ll << lm;
-    const long long half = M / 2;
-    const long long per = half + 1;                   // pairs (k, M-k) for k = 0..M/2
+    const long long per = M / 2 + 1;                 // pairs (k, M-k) for k = 0..M/2
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= count * per) return;
     const long long f = idx / per, k = idx % per;
-    float2* zz = z + f * dist;
-    const float2* twn = tw + 2 * M;                   // level n = 2M
-    if (k == 0) {
-        const float2 z0 = zz[0];
-        zz[0] = real_split(z0, z0, __ldg(twn));
-        zz[M] = real_split(z0, z0, __ldg(twn + M));
-    } else if (k == half) {
-        const float2 zk = zz[k];
-        zz[k] = real_split(zk, zk, __ldg(twn + k));
-    } else {
-        const float2 a = zz[k], b = zz[M - k];
-        zz[k] = real_split(a, b, __ldg(twn + k));
-        zz[M - k] = real_split(b, a, __ldg(twn + (M - k)));
-    }
+    split_pair_inplace<false>(z + f * dist, M, k, tw + 2 * M);
 }
 
 // Y[k] = merge(X[k], X[M-k]) for k < M, written as M complex values.
@@ -163,8 +67,7 @@ __global__ void k_merge(const float2* __restrict__ x, float2* __restrict__ y, lo
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= count * M) return;
     const long long f = idx >> lm, k = idx & (M - 1);
-    const float2* xx = x + f * in_dist;
-    y[f * out_dist + k] = real_merge(__ldcs(xx + k), __ldcs(xx + (M - k)), __ldg(tw + 2 * M + k));
+    merge_elem<false>(x + f * in_dist, y + f * out_dist, M, k, tw + 2 * M);
 }
 
 // ---------------------------------------------------------------- launch

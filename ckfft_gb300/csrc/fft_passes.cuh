@@ -1,0 +1,153 @@
+// fft_passes.cuh -- the two passes of the multi-pass transform as device
+// functions (used by the batched kernels in fft_large.cu and by the persistent
+// job kernel in fft_jobs.cu).
+//
+// N = N1 * N2, x[n] viewed as N1 rows of N2 columns (n = N2*n1 + n2):
+//   columns: for each column n2, Y[k1] = DFT_N1 over n1 of x[N2*n1 + n2], times
+//            W_N^(n2*k1), stored at scratch[N2*k1 + n2];
+//   rows:    for each row k1, DFT_N2 over n2, X[k1 + N1*k2] stored transposed
+//            through shared memory.
+// A tile is C adjacent columns (or rows), so each warp access covers C*8
+// contiguous bytes.  CG selects L2-only loads (ld.global.cg) for data that
+// another CTA wrote earlier in the same launch.
+#pragma once
+#include "fft_core.cuh"
+
+namespace ckg {
+
+// Shape of a sub-transform of 2^LS points inside a pass: R values per thread,
+// C sequences per tile.
+template <int LS>
+struct PassCfg {
+    static constexpr int LOG2R = LS < 4 ? LS : LS <= 10 ? 4 : 5;
+    static constexpr int R = 1 << LOG2R;
+    static constexpr int T = (1 << LS) / R;
+    // at most 512 threads (so up to 128 registers) and ~140 KB of shared memory
+    static constexpr int C = 512 / T < 16 ? 512 / T : 16;
+    static constexpr int THREADS = C * T;
+    // interleaved (pass 1 and pass-2 transpose) and per-row padded (pass 2) layouts
+    static constexpr int INTERLEAVED = (1 << LS) * C + ((1 << LS) * C >> 4) + 1;
+    static constexpr int BLOCKED = C * padded_len(1 << LS);
+    static constexpr int SLOTS = INTERLEAVED > BLOCKED ? INTERLEAVED : BLOCKED;
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)SLOTS;
+};
+
+// Element pos of sequence c in an interleaved tile, padded every 16 slots.
+template <int C>
+struct TileView {
+    float2* base;
+    int c;
+    __device__ __forceinline__ static int slot(int pos, int c) { const int p = pos * C + c; return p + (p >> 4); }
+    __device__ __forceinline__ void st(int pos, float2 x) const { base[slot(pos, c)] = x; }
+    __device__ __forceinline__ float2 ld(int pos) const { return base[slot(pos, c)]; }
+};
+
+template <bool CG>
+__device__ __forceinline__ float2 ld_data(const float2* p)
+{
+    if constexpr (CG) return __ldcg(p);
+    else return __ldcs(p);
+}
+
+// W_N^p for 0 <= p < N = 2^ln from two short table levels:
+// W_N^p = W_{N/2^s}^(p >> s) * W_N^(p mod 2^s), s = ceil(ln/2).
+// Sizes on this path are at most 2^28, so p fits in 32 bits.
+template <bool INV>
+__device__ __forceinline__ float2 big_twiddle(const float2* __restrict__ tw, int ln, int p)
+{
+    const int s = (ln + 1) >> 1;
+    const int hi = p >> s, lo = p & ((1 << s) - 1);
+    const float2 a = __ldg(tw + (1 << (ln - s)) + hi);
+    const float2 b = __ldg(tw + (1 << ln) + lo);
+    const float2 w = cmul(a, b);
+    return INV ? conjf2(w) : w;
+}
+
+// Column pass for tile `tile` of one transform, by threads tid = 0..THREADS-1.
+template <int LA, bool INV, bool CG>
+__device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
+                                          long long tile, int tid, float2* smem, const float2* __restrict__ tw)
+{
+    using P = PassCfg<LA>;
+    const int c = tid % P::C, t = tid / P::C;
+    const long long n2len = 1ll << log2n2;
+    const long long n2 = tile * P::C + c;
+    const float2* src = in + n2;
+    float2 v[P::R];
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) v[m] = ld_data<CG>(src + (long long)(t + m * P::T) * n2len);
+    TileView<P::C> view{smem, c};
+    stockham<LA, P::LOG2R, INV, false>(v, t, tw, view);
+    const int ln = LA + log2n2;
+    float2* dst = out + n2 + (long long)t * n2len;
+    const long long step = (long long)P::T * n2len;
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) {
+        const int k1 = t + m * P::T;
+        __stcs(dst + m * step, cmul(v[m], big_twiddle<INV>(tw, ln, (int)n2 * k1)));
+        // keep the compiler from hoisting every twiddle load ahead of the
+        // stores (that would need 4 more registers per value)
+        if ((m & 3) == 3) asm volatile("" ::: "memory");
+    }
+}
+
+// Row pass for tile `tile` (rows tile*C .. tile*C+C-1) of one transform.
+template <int LB, bool INV, bool CG>
+__device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
+                                          long long tile, int tid, float2* smem, const float2* __restrict__ tw)
+{
+    using P = PassCfg<LB>;
+    constexpr int N2 = 1 << LB;
+    const int r = tid / P::T, t = tid % P::T;
+    const long long n1len = 1ll << log2n1;
+    const long long row0 = tile * P::C;
+    const float2* src = in + (row0 + r) * N2 + t;
+    float2 v[P::R];
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) v[m] = ld_data<CG>(src + m * P::T);
+    PaddedView view{smem + r * padded_len(N2)};
+    stockham<LB, P::LOG2R, INV, (P::T <= 32)>(v, t, tw, view);
+    __syncthreads();
+    // transpose through shared memory so that stores run along rows k1
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) smem[TileView<P::C>::slot(t + m * P::T, r)] = v[m];
+    __syncthreads();
+    const int r2 = tid % P::C, t2 = tid / P::C;
+    float2* dst = out + row0 + r2;
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) {
+        const int k2 = t2 + m * P::T;
+        __stcs(dst + (long long)k2 * n1len, smem[TileView<P::C>::slot(k2, r2)]);
+    }
+}
+
+// Real forward split, in place: pair k in [0, M/2] of a natural-order
+// half-length spectrum z (room for M+1 values) becomes output bins k and M-k
+// (k = 0 gives bins 0 and M; k = M/2 the middle bin).
+template <bool CG>
+__device__ __forceinline__ void split_pair_inplace(float2* __restrict__ z, long long M, long long k,
+                                                   const float2* __restrict__ twn)
+{
+    if (k == 0) {
+        const float2 z0 = ld_data<CG>(z);
+        z[0] = real_split(z0, z0, __ldg(twn));
+        z[M] = real_split(z0, z0, __ldg(twn + M));
+    } else if (k == M / 2) {
+        const float2 zk = ld_data<CG>(z + k);
+        z[k] = real_split(zk, zk, __ldg(twn + k));
+    } else {
+        const float2 a = ld_data<CG>(z + k), b = ld_data<CG>(z + (M - k));
+        z[k] = real_split(a, b, __ldg(twn + k));
+        z[M - k] = real_split(b, a, __ldg(twn + (M - k)));
+    }
+}
+
+// Real inverse merge of element k < M: y[k] from x[k] and x[M-k].
+template <bool CG>
+__device__ __forceinline__ void merge_elem(const float2* __restrict__ x, float2* __restrict__ y, long long M,
+                                           long long k, const float2* __restrict__ twn)
+{
+    y[k] = real_merge(ld_data<CG>(x + k), ld_data<CG>(x + (M - k)), __ldg(twn + k));
+}
+
+}  // namespace ckg

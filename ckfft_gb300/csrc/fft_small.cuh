@@ -65,89 +65,67 @@ __device__ __forceinline__ void split_store(const View& view, float2* __restrict
     }
 }
 
-// ---------------------------------------------------------------- complex
+// ------------------------------------------------------- one-frame bodies
+// The T threads t = 0..T-1 of a group transform one frame between device
+// pointers; `live == false` keeps the group in step (barriers) without
+// touching memory.  Used by the batched kernels below and by the persistent
+// job kernel (fft_jobs.cu).
 
 template <int L, bool INV>
-__global__ void __launch_bounds__(SmallCfg<L>::THREADS, SmallCfg<L>::MINB)
-k_c2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
-            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+__device__ __forceinline__ void frame_c2c(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
+                                          int t, const PaddedView& view, const float2* __restrict__ tw)
 {
     using C = SmallCfg<L>;
-    extern __shared__ float2 smem[];
-    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
-    const long long f = (long long)blockIdx.x * C::TPB + g;
-    const bool live = f < count;
     float2 v[C::R];
     if (live) {
-        const float2* src = in + f * in_dist + t;
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) v[m] = __ldcs(src + m * C::T);
+        for (int m = 0; m < C::R; ++m) v[m] = __ldcs(src + t + m * C::T);
     } else {
 #pragma unroll
         for (int m = 0; m < C::R; ++m) v[m] = make_float2(0.f, 0.f);
     }
-    PaddedView view{smem + g * C::SLOT};
     stockham<L, C::LOG2R, INV, C::WARP>(v, t, tw, view);
     if (live) {
-        float2* dst = out + f * out_dist + t;
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) __stcs(dst + m * C::T, v[m]);
+        for (int m = 0; m < C::R; ++m) __stcs(dst + t + m * C::T, v[m]);
     }
 }
 
-// ------------------------------------------------------------ real forward
-// n = 2M reals -> M+1 complex bins (2 * DFT).  LM = log2 M >= 2.
-
+// Real forward: n = 2M reals (read as M packed pairs) -> M+1 complex bins (2 DFT).
 template <int LM>
-__global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
-k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
-            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+__device__ __forceinline__ void frame_r2c(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
+                                          int t, const PaddedView& view, const float2* __restrict__ tw)
 {
     using C = SmallCfg<LM>;
     constexpr int M = 1 << LM;
-    extern __shared__ float2 smem[];
-    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
-    const long long f = (long long)blockIdx.x * C::TPB + g;
-    const bool live = f < count;
     float2 v[C::R];
     if (live) {
-        const float2* src = in + f * in_dist + t;      // packed pairs (x[2p], x[2p+1])
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) v[m] = __ldcs(src + m * C::T);
+        for (int m = 0; m < C::R; ++m) v[m] = __ldcs(src + t + m * C::T);
     } else {
 #pragma unroll
         for (int m = 0; m < C::R; ++m) v[m] = make_float2(0.f, 0.f);
     }
-    PaddedView view{smem + g * C::SLOT};
     stockham<LM, C::LOG2R, false, C::WARP>(v, t, tw, view);
     // natural-order half-size spectrum Z to shared memory, then split
 #pragma unroll
     for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, v[m]);
     xsync<C::WARP>();
-    if (live) split_store<C, M>(view, out + f * out_dist, t, tw + 2 * M);
+    if (live) split_store<C, M>(view, dst, t, tw + 2 * M);
 }
 
-// ------------------------------------------------------------ real inverse
-// M+1 complex bins -> n = 2M reals.
-
+// Real inverse: M+1 complex bins -> n = 2M reals (written as M packed pairs).
 template <int LM>
-__global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
-k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
-            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+__device__ __forceinline__ void frame_c2r(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
+                                          int t, const PaddedView& view, const float2* __restrict__ tw)
 {
     using C = SmallCfg<LM>;
     constexpr int M = 1 << LM;
-    extern __shared__ float2 smem[];
-    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
-    const long long f = (long long)blockIdx.x * C::TPB + g;
-    const bool live = f < count;
-    PaddedView view{smem + g * C::SLOT};
     const float2* twn = tw + 2 * M;
     float2 v[C::R];
     if (live) {
         // both merge operands straight from HBM: X[p] coalesced ascending and
         // X[M-p] coalesced descending (the second read of each line hits cache)
-        const float2* src = in + f * in_dist;
         float2 a[C::R], b[C::R];
 #pragma unroll
         for (int m = 0; m < C::R; ++m) {
@@ -165,10 +143,47 @@ k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
     }
     stockham<LM, C::LOG2R, true, C::WARP>(v, t, tw, view);
     if (live) {
-        float2* dst = out + f * out_dist + t;
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) __stcs(dst + m * C::T, v[m]);
+        for (int m = 0; m < C::R; ++m) __stcs(dst + t + m * C::T, v[m]);
     }
+}
+
+// ------------------------------------------------------------ batched kernels
+
+template <int L, bool INV>
+__global__ void __launch_bounds__(SmallCfg<L>::THREADS, SmallCfg<L>::MINB)
+k_c2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
+            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+{
+    using C = SmallCfg<L>;
+    extern __shared__ float2 smem[];
+    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const long long f = (long long)blockIdx.x * C::TPB + g;
+    frame_c2c<L, INV>(in + f * in_dist, out + f * out_dist, f < count, t, PaddedView{smem + g * C::SLOT}, tw);
+}
+
+template <int LM>
+__global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
+k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
+            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+{
+    using C = SmallCfg<LM>;
+    extern __shared__ float2 smem[];
+    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const long long f = (long long)blockIdx.x * C::TPB + g;
+    frame_r2c<LM>(in + f * in_dist, out + f * out_dist, f < count, t, PaddedView{smem + g * C::SLOT}, tw);
+}
+
+template <int LM>
+__global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
+k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
+            long long in_dist, long long out_dist, const float2* __restrict__ tw)
+{
+    using C = SmallCfg<LM>;
+    extern __shared__ float2 smem[];
+    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const long long f = (long long)blockIdx.x * C::TPB + g;
+    frame_c2r<LM>(in + f * in_dist, out + f * out_dist, f < count, t, PaddedView{smem + g * C::SLOT}, tw);
 }
 
 // ---------------------------------------------------------------- launch

@@ -1,0 +1,84 @@
+// jobs.h -- work-unit descriptors of the persistent job kernel (host and device).
+//
+// A run of mixed transforms is flattened into a queue of units that the
+// persistent CTAs pop with one atomic add each:
+//   * single-CTA units: up to 512/T frames of one kind and size, each frame
+//     with its own input / output pointer (FrameDesc);
+//   * phase units of a multi-pass transform (LargeDesc): a merge range, a set
+//     of column tiles, a set of row tiles, or a split range.  A phase unit
+//     names how many units of its transform must have finished first; every
+//     unit of a transform adds one to that transform's counter when done.
+// Phase-p units are queued after every phase-(p-1) unit, so a CTA only ever
+// waits for units that CTAs already running have taken.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ckg {
+
+enum UnitOp : int {
+    U_C2C_FWD = 0,     // single-CTA complex forward, log2a = log2 n
+    U_C2C_INV = 1,
+    U_R2C = 2,         // single-CTA real forward, log2a = log2 (n/2)
+    U_C2R = 3,
+    U_RTINY_FWD = 4,   // real n = 1, 2, 4 closed forms, log2a = log2 n
+    U_RTINY_INV = 5,
+    U_COLS_FWD = 6,    // column pass, log2a = column length, log2b = log2 columns
+    U_COLS_INV = 7,
+    U_ROWS_FWD = 8,    // row pass, log2a = row length, log2b = log2 rows
+    U_ROWS_INV = 9,
+    U_SPLIT = 10,      // real forward split in place, log2a = log2 (n/2)
+    U_MERGE = 11,      // real inverse merge, log2a = log2 (n/2)
+};
+
+// Buffer selectors of a phase unit.
+enum BufSel : int { B_IN = 0, B_OUT = 1, B_SCRATCH = 2 };
+
+struct Unit {
+    int op;
+    int log2a;
+    int log2b;
+    int job;       // LargeDesc index, -1 for single-CTA units
+    int need;      // units of `job` that must have finished before this one
+    int first;     // first frame (single), first tile (pass), first element (split / merge)
+    int count;     // frames, tiles or elements
+    int sel;       // source selector | destination selector << 4 (phase units)
+};
+
+struct FrameDesc {
+    const float2* in;
+    float2* out;
+};
+
+struct LargeDesc {
+    const float2* in;
+    float2* out;
+    float2* scratch;
+    long long pad;
+};
+
+struct JobsArgs {
+    const Unit* units;
+    int nunits;
+    const FrameDesc* frames;
+    const LargeDesc* large;
+    int* done;         // one counter per LargeDesc
+    int* head;         // queue head
+    const float2* tw;
+    unsigned* err;
+};
+
+constexpr int kJobThreads = 512;
+
+// Largest multi-pass size the job kernel handles (sub-lengths up to 2^10).
+constexpr int kJobMaxLog2Complex = 20;
+// Single-CTA sizes inside the job kernel (complex length, 64 registers).
+constexpr int kJobMaxSingleLog2 = 13;
+
+// Launches the job kernel on all resident CTAs of the current device.
+cudaError_t launch_jobs(const JobsArgs& a, cudaStream_t s);
+// Shared memory the job kernel needs (bytes) and resident CTAs per SM.
+size_t jobs_smem_bytes();
+int jobs_grid();
+
+}  // namespace ckg

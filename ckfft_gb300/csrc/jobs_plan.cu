@@ -1,0 +1,422 @@
+// jobs_plan.cu -- host side of mixed runs: CkFftCudaPlanJobs / ExecPlan / RunJobs.
+//
+// Turns a list of jobs (kind, size, count, device pointers) into the unit
+// queue of the persistent job kernel (jobs.h), uploads it once, and captures
+// "reset counters + persistent launch" into a CUDA graph, so a replay costs one
+// graph launch regardless of how many transforms the run holds.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ckfft_cuda.h"
+#include "fft_passes.cuh"
+#include "fft_small.cuh"
+#include "jobs.h"
+#include "kernels.h"
+
+namespace ckg {
+
+struct ContextView {
+    int nmax;
+    int direction;
+    int device;
+    const float2* tw;
+};
+bool context_view(const CkFftContext* c, ContextView* out);
+void set_last_error(const char* msg);
+
+// Threads per tile and tiles per pass unit for sub-length 2^LS (PassCfg).
+struct PassShape {
+    int threads;
+    int cols;
+};
+static PassShape pass_shape(int ls)
+{
+    switch (ls) {
+    case 7: return {PassCfg<7>::THREADS, PassCfg<7>::C};
+    case 8: return {PassCfg<8>::THREADS, PassCfg<8>::C};
+    case 9: return {PassCfg<9>::THREADS, PassCfg<9>::C};
+    case 10: return {PassCfg<10>::THREADS, PassCfg<10>::C};
+    default: return {0, 0};
+    }
+}
+
+// Threads per frame of a single-CTA size 2^L (SmallCfg<L>::T).
+static int single_threads(int l)
+{
+    switch (l) {
+    case 0: return SmallCfg<0>::T;
+    case 1: return SmallCfg<1>::T;
+    case 2: return SmallCfg<2>::T;
+    case 3: return SmallCfg<3>::T;
+    case 4: return SmallCfg<4>::T;
+    case 5: return SmallCfg<5>::T;
+    case 6: return SmallCfg<6>::T;
+    case 7: return SmallCfg<7>::T;
+    case 8: return SmallCfg<8>::T;
+    case 9: return SmallCfg<9>::T;
+    case 10: return SmallCfg<10>::T;
+    case 11: return SmallCfg<11>::T;
+    case 12: return SmallCfg<12>::T;
+    case 13: return SmallCfg<13>::T;
+    default: return 0;
+    }
+}
+
+constexpr int kElemsPerUnit = kJobThreads * 8;   // split / merge work per unit
+
+struct Built {
+    std::vector<Unit> units;
+    std::vector<FrameDesc> frames;
+    std::vector<LargeDesc> large;   // scratch pointers relative (offset in float2) until placed
+    std::vector<long long> scratch_off;
+    long long scratch_elems = 0;
+    long long algo_bytes = 0;
+    long long transforms = 0;
+};
+
+static int ilog2ll(long long n)
+{
+    int l = 0;
+    while ((1ll << l) < n) ++l;
+    return l;
+}
+
+static bool on_device(const void* p, int dev)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
+// Validates the jobs and builds the unit queue.  Returns false with an error set.
+static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, Built* b)
+{
+    if (njobs < 0 || (njobs > 0 && !jobs)) {
+        set_last_error("jobs must be a non-NULL array when njobs > 0");
+        return false;
+    }
+    std::map<std::pair<int, int>, std::vector<FrameDesc>> buckets;   // (op, log2a) -> frames
+    std::vector<std::vector<Unit>> phase(3);
+    for (int j = 0; j < njobs; ++j) {
+        const CkFftCudaJob& J = jobs[j];
+        char msg[200];
+        if (J.kind < 0 || J.kind > 3) {
+            snprintf(msg, sizeof msg, "job %d: kind must be 0..3", j);
+            set_last_error(msg);
+            return false;
+        }
+        const bool inverse = J.kind == 1 || J.kind == 3;
+        const bool real = J.kind >= 2;
+        if (!(cv.direction & (inverse ? kCkFftDirection_Inverse : kCkFftDirection_Forward))) {
+            snprintf(msg, sizeof msg, "job %d: context was created without this direction", j);
+            set_last_error(msg);
+            return false;
+        }
+        if (J.n <= 0 || (J.n & (J.n - 1)) || J.n > cv.nmax) {
+            snprintf(msg, sizeof msg, "job %d: n must be a power of two no larger than the context's nMax", j);
+            set_last_error(msg);
+            return false;
+        }
+        if (J.count < 0) {
+            snprintf(msg, sizeof msg, "job %d: count must be >= 0", j);
+            set_last_error(msg);
+            return false;
+        }
+        if (J.count == 0) continue;
+        if (!J.input || !J.output || J.input == J.output) {
+            snprintf(msg, sizeof msg, "job %d: input and output must be distinct non-NULL buffers", j);
+            set_last_error(msg);
+            return false;
+        }
+        if (!on_device(J.input, cv.device) || !on_device(J.output, cv.device)) {
+            snprintf(msg, sizeof msg, "job %d: jobs take device (or managed) memory", j);
+            set_last_error(msg);
+            return false;
+        }
+        if (((uintptr_t)J.input & 7) || ((uintptr_t)J.output & 7)) {
+            snprintf(msg, sizeof msg, "job %d: device buffers must be 8-byte aligned", j);
+            set_last_error(msg);
+            return false;
+        }
+        const int L = ilog2ll(J.n);
+        const int lc = real ? L - 1 : L;                     // complex (half-)length
+        if (lc > kJobMaxLog2Complex) {
+            snprintf(msg, sizeof msg, "job %d: n = %d exceeds the job kernel's limit (complex 2^20, real 2^21)", j, J.n);
+            set_last_error(msg);
+            return false;
+        }
+        const long long in_dist = real ? (inverse ? J.n / 2 + 1 : J.n / 2) : J.n;    // float2 units
+        const long long out_dist = real ? (inverse ? J.n / 2 : J.n / 2 + 1) : J.n;
+        const long long in_stride_bytes = real && !inverse ? 4ll * J.n : 8ll * in_dist;
+        const long long out_stride_bytes = real && inverse ? 4ll * J.n : 8ll * out_dist;
+        b->algo_bytes += (long long)J.count * (real ? 4ll * J.n + 8ll * (J.n / 2 + 1) : 16ll * J.n);
+        b->transforms += J.count;
+        for (int f = 0; f < J.count; ++f) {
+            const float2* in = (const float2*)((const char*)J.input + (size_t)f * in_stride_bytes);
+            float2* out = (float2*)((char*)J.output + (size_t)f * out_stride_bytes);
+            if (real && J.n <= 4) {
+                buckets[{inverse ? U_RTINY_INV : U_RTINY_FWD, L}].push_back({in, out});
+            } else if (lc <= kJobMaxSingleLog2) {
+                const int op = real ? (inverse ? U_C2R : U_R2C) : (inverse ? U_C2C_INV : U_C2C_FWD);
+                buckets[{op, lc}].push_back({in, out});
+            } else {
+                // multi-pass transform: phases of column / row tiles (+ merge or split)
+                const int job = (int)b->large.size();
+                b->large.push_back({in, out, nullptr, 0});
+                b->scratch_off.push_back(b->scratch_elems);
+                b->scratch_elems += 1ll << lc;
+                const int la = lc / 2, lb = lc - la;
+                const PassShape pa = pass_shape(la), pb = pass_shape(lb);
+                const int sa = kJobThreads / pa.threads, sb = kJobThreads / pb.threads;
+                const int tiles_a = (1 << lb) / pa.cols, tiles_b = (1 << la) / pb.cols;
+                int done = 0, p = 0, added = 0;   // units of earlier phases, of this phase
+                auto add_pass = [&](int op, int ls, int other, int tiles, int per, int src, int dst) {
+                    for (int t = 0; t < tiles; t += per, ++added)
+                        phase[p].push_back({op, ls, other, job, done, t, per, src | (dst << 4)});
+                };
+                auto add_elems = [&](int op, long long count, int src, int dst) {
+                    for (long long e = 0; e < count; e += kElemsPerUnit, ++added)
+                        phase[p].push_back({op, lc, 0, job, done, (int)e, (int)std::min<long long>(kElemsPerUnit, count - e), src | (dst << 4)});
+                };
+                auto end_phase = [&]() {
+                    done += added;
+                    added = 0;
+                    ++p;
+                };
+                if (real && inverse) {
+                    add_elems(U_MERGE, 1ll << lc, B_IN, B_OUT);
+                    end_phase();
+                    add_pass(U_COLS_INV, la, lb, tiles_a, sa, B_OUT, B_SCRATCH);
+                    end_phase();
+                    add_pass(U_ROWS_INV, lb, la, tiles_b, sb, B_SCRATCH, B_OUT);
+                } else {
+                    add_pass(inverse ? U_COLS_INV : U_COLS_FWD, la, lb, tiles_a, sa, B_IN, B_SCRATCH);
+                    end_phase();
+                    add_pass(inverse ? U_ROWS_INV : U_ROWS_FWD, lb, la, tiles_b, sb, B_SCRATCH, B_OUT);
+                    if (real) {
+                        end_phase();
+                        add_elems(U_SPLIT, (1ll << lc) / 2 + 1, B_OUT, B_OUT);
+                    }
+                }
+            }
+        }
+    }
+    // queue: first phase of every multi-pass transform, then the single-CTA
+    // units (largest frames first), then the later phases in order
+    b->units = phase[0];
+    std::vector<std::pair<std::pair<int, int>, std::vector<FrameDesc>>> order(buckets.begin(), buckets.end());
+    std::stable_sort(order.begin(), order.end(), [](const auto& x, const auto& y) { return x.first.second > y.first.second; });
+    for (auto& kv : order) {
+        const int op = kv.first.first, l2 = kv.first.second;
+        const int per = (op == U_RTINY_FWD || op == U_RTINY_INV) ? kJobThreads : kJobThreads / single_threads(l2);
+        const std::vector<FrameDesc>& fr = kv.second;
+        for (size_t i = 0; i < fr.size(); i += per) {
+            const int cnt = (int)std::min<size_t>(per, fr.size() - i);
+            b->units.push_back({op, l2, 0, -1, 0, (int)b->frames.size(), cnt, 0});
+            b->frames.insert(b->frames.end(), fr.begin() + i, fr.begin() + i + cnt);
+        }
+    }
+    b->units.insert(b->units.end(), phase[1].begin(), phase[1].end());
+    b->units.insert(b->units.end(), phase[2].begin(), phase[2].end());
+    return true;
+}
+
+}  // namespace ckg
+
+using namespace ckg;
+
+struct _CkFftCudaPlan {
+    ContextView cv;
+    int nunits = 0;
+    int nlarge = 0;
+    void* dmem = nullptr;        // units | frames | large | done | head
+    float2* scratch = nullptr;
+    JobsArgs args{};
+    size_t counters_bytes = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long algo_bytes = 0;
+    long long transforms = 0;
+};
+
+namespace {
+
+template <class T>
+size_t align_up(size_t x) { return (x + alignof(T) - 1) / alignof(T) * alignof(T); }
+
+// Lays out the built queue in one device allocation.  `dmem` receives the
+// allocation, `scratch` the multi-pass intermediates.
+cudaError_t upload(const Built& b, ContextView cv, void** dmem, float2** scratch, JobsArgs* a, size_t* counters_bytes,
+                   cudaStream_t s, bool async_alloc)
+{
+    size_t off = 0;
+    const size_t o_units = off; off += sizeof(Unit) * b.units.size();
+    off = (off + 15) / 16 * 16;
+    const size_t o_frames = off; off += sizeof(FrameDesc) * b.frames.size();
+    off = (off + 15) / 16 * 16;
+    const size_t o_large = off; off += sizeof(LargeDesc) * b.large.size();
+    off = (off + 15) / 16 * 16;
+    const size_t o_done = off; off += sizeof(int) * (b.large.size() + 1);   // + queue head
+    const size_t total = off + 16;
+    cudaError_t e = async_alloc ? cudaMallocAsync(dmem, total, s) : cudaMalloc(dmem, total);
+    if (e != cudaSuccess) return e;
+    *scratch = nullptr;
+    if (b.scratch_elems) {
+        e = async_alloc ? cudaMallocAsync((void**)scratch, sizeof(float2) * b.scratch_elems, s)
+                        : cudaMalloc((void**)scratch, sizeof(float2) * b.scratch_elems);
+        if (e != cudaSuccess) return e;
+    }
+    std::vector<char> host(total, 0);
+    memcpy(host.data() + o_units, b.units.data(), sizeof(Unit) * b.units.size());
+    memcpy(host.data() + o_frames, b.frames.data(), sizeof(FrameDesc) * b.frames.size());
+    std::vector<LargeDesc> large = b.large;
+    for (size_t i = 0; i < large.size(); ++i) large[i].scratch = *scratch + b.scratch_off[i];
+    memcpy(host.data() + o_large, large.data(), sizeof(LargeDesc) * large.size());
+    // pageable source: the call returns once the data is staged, so `host` may go
+    e = cudaMemcpyAsync(*dmem, host.data(), total, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    char* base = (char*)*dmem;
+    a->units = (const Unit*)(base + o_units);
+    a->nunits = (int)b.units.size();
+    a->frames = (const FrameDesc*)(base + o_frames);
+    a->large = (const LargeDesc*)(base + o_large);
+    a->done = (int*)(base + o_done);
+    a->head = a->done + b.large.size();
+    a->tw = cv.tw;
+    a->err = device_error_word();
+    *counters_bytes = sizeof(int) * (b.large.size() + 1);
+    return cudaSuccess;
+}
+
+int fail_cuda(const char* where, cudaError_t e)
+{
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    set_last_error(m.c_str());
+    return 0;
+}
+
+struct DevScope {
+    int prev = -1;
+    bool ok = true;
+    explicit DevScope(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) { ok = false; return; }
+        if (prev != dev && cudaSetDevice(dev) != cudaSuccess) ok = false;
+    }
+    ~DevScope() { if (prev >= 0) cudaSetDevice(prev); }
+};
+
+}  // namespace
+
+extern "C" {
+
+CkFftCudaPlan* CkFftCudaPlanJobs(CkFftContext* context, const CkFftCudaJob* jobs, int njobs)
+{
+    ContextView cv;
+    if (!context_view(context, &cv)) { set_last_error("NULL or invalid context"); return nullptr; }
+    DevScope scope(cv.device);
+    if (!scope.ok) { set_last_error("cannot select the context's device"); return nullptr; }
+    Built b;
+    if (!build_units(cv, jobs, njobs, &b)) return nullptr;
+    CkFftCudaPlan* p = new (std::nothrow) _CkFftCudaPlan();
+    if (!p) { set_last_error("out of host memory"); return nullptr; }
+    p->cv = cv;
+    p->nunits = (int)b.units.size();
+    p->nlarge = (int)b.large.size();
+    p->algo_bytes = b.algo_bytes;
+    p->transforms = b.transforms;
+    cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = upload(b, cv, &p->dmem, &p->scratch, &p->args, &p->counters_bytes, p->stream, false);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e == cudaSuccess && p->nunits > 0) {
+        e = cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e1 = cudaMemsetAsync(p->args.done, 0, p->counters_bytes, p->stream);
+            cudaError_t e2 = e1 == cudaSuccess ? launch_jobs(p->args, p->stream) : e1;
+            e = cudaStreamEndCapture(p->stream, &p->graph);
+            if (e == cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+    }
+    if (e != cudaSuccess) {
+        fail_cuda("planning the job run", e);
+        CkFftCudaDestroyPlan(p);
+        return nullptr;
+    }
+    return p;
+}
+
+int CkFftCudaExecPlan(CkFftCudaPlan* p, void* stream)
+{
+    if (!p) { set_last_error("NULL plan"); return 0; }
+    if (p->nunits == 0) return 1;
+    DevScope scope(p->cv.device);
+    if (!scope.ok) { set_last_error("cannot select the plan's device"); return 0; }
+    cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
+    cudaError_t e = cudaGraphLaunch(p->exec, s);
+    if (e != cudaSuccess) return fail_cuda("cudaGraphLaunch", e);
+    count_launch();
+    if (!stream) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail_cuda("cudaStreamSynchronize", e);
+        if (take_device_error()) { set_last_error("a job kernel wait timed out"); return 0; }
+    }
+    return 1;
+}
+
+void CkFftCudaDestroyPlan(CkFftCudaPlan* p)
+{
+    if (!p) return;
+    DevScope scope(p->cv.device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    cudaFree(p->dmem);
+    cudaFree(p->scratch);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+long long CkFftCudaPlanBytes(const CkFftCudaPlan* p) { return p ? p->algo_bytes : 0; }
+
+int CkFftCudaRunJobs(CkFftContext* context, const CkFftCudaJob* jobs, int njobs, void* stream)
+{
+    ContextView cv;
+    if (!context_view(context, &cv)) { set_last_error("NULL or invalid context"); return 0; }
+    DevScope scope(cv.device);
+    if (!scope.ok) { set_last_error("cannot select the context's device"); return 0; }
+    Built b;
+    if (!build_units(cv, jobs, njobs, &b)) return 0;
+    if (b.units.empty()) return 1;
+    cudaStream_t s = (cudaStream_t)stream;
+    void* dmem = nullptr;
+    float2* scratch = nullptr;
+    JobsArgs a{};
+    size_t cb = 0;
+    cudaError_t e = upload(b, cv, &dmem, &scratch, &a, &cb, s, true);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.done, 0, cb, s);
+    if (e == cudaSuccess) {
+        e = launch_jobs(a, s);
+        if (e == cudaSuccess) count_launch();
+    }
+    if (dmem) cudaFreeAsync(dmem, s);
+    if (scratch) cudaFreeAsync(scratch, s);
+    if (e != cudaSuccess) return fail_cuda("job run", e);
+    if (!stream) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail_cuda("cudaStreamSynchronize", e);
+        if (take_device_error()) { set_last_error("a job kernel wait timed out"); return 0; }
+    }
+    return 1;
+}
+
+}  // extern "C"

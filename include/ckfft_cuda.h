@@ -5,7 +5,7 @@
  * names, signatures, argument meaning, scaling and return codes as the
  * reference's public header (inc/ckfft/ckfft.h).  A program written against
  * the reference links unchanged against libckfft_cuda.so.  The header compiles
- * as C89/C99 as well as C++.
+ * as C99 or later and as C++.
  *
  * Pointers given to any entry point may be host memory (pageable or pinned) or
  * device memory (cudaMalloc / cudaMallocManaged) on the context's device; the
@@ -119,6 +119,53 @@ int CkFftCudaRealInverseBatch(CkFftContext* context, int n, int count,
 /* Number of kernel launches the library has issued in this process (all
  * contexts, all threads).  Lets a caller count launches inside a timed region. */
 long long CkFftCudaLaunchCount(void);
+
+/* ----------------------------------------------------------------------
+ * Mixed runs: many transforms of different sizes, kinds and directions in
+ * one persistent kernel launch (no counterpart in the reference).
+ * ---------------------------------------------------------------------- */
+
+#define CKFFT_CUDA_COMPLEX_FORWARD 0
+#define CKFFT_CUDA_COMPLEX_INVERSE 1
+#define CKFFT_CUDA_REAL_FORWARD    2
+#define CKFFT_CUDA_REAL_INVERSE    3
+
+/* One job: `count` transforms of size n stored back to back, laid out as in
+ * the batch calls.  input / output are device (or managed) memory on the
+ * context's device, 8-byte aligned.  Jobs of one run must not write memory
+ * that another job of the run reads.  Complex n up to 2^20, real n up to 2^21. */
+typedef struct
+{
+    int kind;             /* CKFFT_CUDA_COMPLEX_FORWARD .. CKFFT_CUDA_REAL_INVERSE */
+    int n;
+    int count;
+    const void* input;
+    void* output;
+}
+CkFftCudaJob;
+
+typedef struct _CkFftCudaPlan CkFftCudaPlan;
+
+/* Validates the jobs (same rules and errors as the single calls), builds the
+ * device work queue, allocates the multi-pass intermediates and captures the
+ * run into a CUDA graph.  Returns NULL on error (see CkFftCudaGetLastError). */
+CkFftCudaPlan* CkFftCudaPlanJobs(CkFftContext* context, const CkFftCudaJob* jobs, int njobs);
+
+/* Replays a plan: one graph launch.  stream NULL blocks until done; otherwise
+ * the replay is enqueued on that cudaStream_t.  Replays of one plan must not
+ * overlap each other (they share the plan's queue and counters). */
+int CkFftCudaExecPlan(CkFftCudaPlan* plan, void* stream);
+
+/* Frees a plan (waits for its work). */
+void CkFftCudaDestroyPlan(CkFftCudaPlan* plan);
+
+/* Algorithmic HBM bytes of one replay of the plan (each transform read once
+ * and written once). */
+long long CkFftCudaPlanBytes(const CkFftCudaPlan* plan);
+
+/* One-shot mixed run without a graph: plan, launch, free (stream-ordered).
+ * stream NULL blocks until done. */
+int CkFftCudaRunJobs(CkFftContext* context, const CkFftCudaJob* jobs, int njobs, void* stream);
 
 /* Complex batch that allocates no memory.  No counterpart in the reference.
  * For callers that must not allocate while they run: a real-time audio
