@@ -53,6 +53,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-percall", action="store_true")
+    ap.add_argument("--workload", choices=["w1", "w2", "w3", "w4", "w5"], default="w2",
+                    help="w2 (default): real n=4096 x 65536 frames; w1: complex n=1024 x 4096 round trip; "
+                         "w3: large single complex transforms; w4: uneven mixed batch; w5: serving")
     return ap.parse_args()
 
 
@@ -380,8 +383,260 @@ def measure_per_call(torch, ctx, x, n, calls=512):
             "calls": calls, "api": "CkFftRealForward per frame (device pointers, blocking)"}
 
 
+# ------------------------------------------------------------ other workloads
+
+def l2_flusher(torch, dev):
+    """Between timed steps, outside the events: writes a buffer twice the L2 size,
+    then reads another one, so L2 holds clean lines (no write-back of the flush
+    buffer lands inside the next timed step)."""
+    wbuf = torch.empty(64 << 20, dtype=torch.float32, device=dev)     # 256 MiB
+    rbuf = torch.ones(64 << 20, dtype=torch.float32, device=dev)
+
+    def flush():
+        wbuf.fill_(1.0)
+        rbuf.sum()
+    return flush
+
+
+def timed_steps(torch, stream, step, steps, flush=None):
+    """Per-step CUDA-event time on `stream` (flush, if any, runs outside the events)."""
+    total = 0.0
+    for _ in range(steps):
+        if flush:
+            flush()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        total += a.elapsed_time(b) / 1e3
+    return total
+
+
+def base_line(args, metric, value, unit, secs, config, world=1):
+    return {"metric": metric, "value": round(value, 2), "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(secs / args.steps * 1e3, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": config}
+
+
+def run_w1(args):
+    """Workload 1: complex forward then inverse, n = 1024, 4096 frames, U[-1,1) seed 0."""
+    import torch
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+
+    n, frames = wl.W1_N, wl.W1_FRAMES
+    ctx = binding.Context(n)
+    x = torch.from_numpy(wl.complex_uniform(frames, n, wl.W1_SEED)).cuda()
+    X, y = torch.empty_like(x), torch.empty_like(x)
+    stream = torch.cuda.Stream()
+    fwd_ev = []
+
+    def step():
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.check(ctx.batch("cfwd", n, frames, x, X, stream))
+        b.record(stream)
+        fwd_ev.append((a, b))
+        ctx.check(ctx.batch("cinv", n, frames, X, y, stream))
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    err = (torch.linalg.vector_norm(y / n - x) / torch.linalg.vector_norm(x)).item()
+    fwd_ev.clear()
+    flush = l2_flusher(torch, x.device)
+    launches0 = binding.launch_count()
+    secs = timed_steps(torch, stream, step, args.steps, flush)
+    launches = binding.launch_count() - launches0
+    per = 16 * n
+    value = args.steps * 2 * frames * per / secs / 1e9
+    fwd_ms = sum(a.elapsed_time(b) for a, b in fwd_ev) / len(fwd_ev)
+    peak, src = measured_peaks()
+    line = base_line(args, "batched complex FFT GB/s (N=1024 FP32, fwd+inv)", value, "GB/s", secs,
+                     {"workload": f"complex FFT n={n}, {frames} frames, forward then inverse (round trip)",
+                      "n": n, "frames": frames, "l2": "256 MiB buffer written between timed steps (outside the events)"})
+    line["roofline"] = {"bound": "hbm", "kernel": "k_c2c_small<10> (complex forward, n=1024)",
+                        "achieved": round(frames * per / (fwd_ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(frames * per / (fwd_ms / 1e3) / 1e9 / peak, 4), "peak_source": src,
+                        "traffic": None, "avg_launch_ms": round(fwd_ms, 4)}
+    line["gpu_launches"] = launches
+    line["round_trip_rel_err"] = err
+    line["transforms_per_s"] = round(args.steps * 2 * frames / secs, 1)
+    if not args.no_e2e:
+        xh = x.cpu().pin_memory()
+        Xh = torch.empty_like(xh).pin_memory()
+        yh = torch.empty_like(xh).pin_memory()
+        ctx.check(ctx.batch("cfwd", n, frames, xh, Xh))
+        t0 = time.perf_counter()
+        for _ in range(3):
+            ctx.check(ctx.batch("cfwd", n, frames, xh, Xh))
+            ctx.check(ctx.batch("cinv", n, frames, Xh, yh))
+        dt = (time.perf_counter() - t0) / 3
+        line["e2e"] = {"value": round(2 * frames * per / dt / 1e9, 2), "unit": "GB/s",
+                       "h2d_bytes_per_step": 2 * frames * n * 8, "d2h_bytes_per_step": 2 * frames * n * 8,
+                       "ms_per_step": round(dt * 1e3, 3)}
+    if not args.no_cpu:
+        line["cpu_baseline"] = time_cpu_complex(n, frames)
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def time_cpu_complex(n, frames, min_seconds=2.0):
+    import numpy as np
+    from oracle import oracle as orc
+    from ckfft_gb300 import workloads as wl
+
+    orc.build(with_reference=False)
+    threads = os.cpu_count() or 1
+    x = wl.complex_uniform(frames, n, 0)
+    X = np.empty_like(x)
+    y = np.empty_like(x)
+    o = orc.Oracle(n, fast=True)
+    o.batch_into(orc.KIND_CFWD, n, frames, x, X, threads)
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < min_seconds:
+        o.batch_into(orc.KIND_CFWD, n, frames, x, X, threads)
+        o.batch_into(orc.KIND_CINV, n, frames, X, y, threads)
+        done += frames
+    dt = time.perf_counter() - t0
+    return {"value": round(done * 2 * 16 * n / dt / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "transforms_per_s": round(2 * done / dt, 1),
+            "sample": f"{frames} frames of n={n}, forward+inverse, repeated for {dt:.2f} s on {threads} threads"}
+
+
+def run_w3(args):
+    """Workload 3: single complex transforms of 2^20, 2^22, 2^24 points, N(0,1), fwd + inv."""
+    import numpy as np
+    import torch
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+    from oracle import oracle as orc
+
+    ctx = binding.Context(1 << 24)
+    stream = torch.cuda.Stream()
+    flush = l2_flusher(torch, torch.device("cuda"))
+    peak, src = measured_peaks()
+    sizes = {}
+    for l2 in wl.W3_LOG2:
+        n = 1 << l2
+        xh = wl.complex_normal(n, seed=l2)
+        x = torch.from_numpy(xh).cuda()
+        X, y = torch.empty_like(x), torch.empty_like(x)
+
+        def step():
+            ctx.check(ctx.batch("cfwd", n, 1, x, X, stream))
+            ctx.check(ctx.batch("cinv", n, 1, X, y, stream))
+
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize()
+        fwd_err = float(np.linalg.norm(X.cpu().numpy() - np.fft.fft(xh.astype(np.complex128))) /
+                        np.linalg.norm(np.fft.fft(xh.astype(np.complex128))))
+        rt_err = (torch.linalg.vector_norm(y / n - x) / torch.linalg.vector_norm(x)).item()
+        secs = timed_steps(torch, stream, step, args.steps, flush)
+        gbs = args.steps * 2 * 16 * n / secs / 1e9
+        sizes[f"2^{l2}"] = {"gbs_algorithmic": round(gbs, 1), "gbs_two_pass_traffic": round(2 * gbs, 1),
+                            "frac_of_peak_two_pass": round(2 * gbs / peak, 4),
+                            "us_per_transform": round(secs / (2 * args.steps) * 1e6, 2),
+                            "rel_err_fwd_vs_fp64": fwd_err, "round_trip_rel_err": rt_err}
+        del x, X, y
+    top = sizes[f"2^{max(wl.W3_LOG2)}"]
+    line = base_line(args, "large complex FFT GB/s (2^24 points, fwd+inv)", top["gbs_algorithmic"], "GB/s",
+                     top["us_per_transform"] * 2 * args.steps / 1e6,
+                     {"workload": "single complex transforms of 2^20, 2^22, 2^24 points, N(0,1), forward + inverse",
+                      "l2": "256 MiB buffer written between timed steps (outside the events)", "passes": 2})
+    line["sizes"] = sizes
+    line["roofline"] = {"bound": "hbm", "kernel": "k_cols + k_rows (two passes, 16 n bytes each)",
+                        "achieved": top["gbs_two_pass_traffic"], "peak": peak, "unit": "GB/s",
+                        "frac": top["frac_of_peak_two_pass"], "peak_source": src, "traffic": None}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_w4(args):
+    """Workload 4: 10000 transforms of uneven sizes in one graph-captured persistent launch,
+    against the plain path of one CkFft* call per transform."""
+    import numpy as np
+    import torch
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+
+    spec = wl.uneven_jobs()
+    ctx = binding.Context(1 << 16)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(wl.W4_SEED)
+    jobs = []
+    for real, inv, l2 in spec:
+        n = 1 << l2
+        if real and not inv:
+            x = torch.rand(n, generator=g, device="cuda") * 2 - 1
+            y = torch.empty(n // 2 + 1, dtype=torch.complex64, device="cuda")
+            kind = "rfwd"
+        elif real:
+            x = torch.complex(torch.rand(n // 2 + 1, generator=g, device="cuda") * 2 - 1,
+                              torch.rand(n // 2 + 1, generator=g, device="cuda") * 2 - 1)
+            y = torch.empty(n, device="cuda")
+            kind = "rinv"
+        else:
+            x = torch.complex(torch.rand(n, generator=g, device="cuda") * 2 - 1,
+                              torch.rand(n, generator=g, device="cuda") * 2 - 1)
+            y = torch.empty_like(x)
+            kind = "cinv" if inv else "cfwd"
+        jobs.append((kind, n, 1, x, y))
+    plan = ctx.plan(jobs)
+    stream = torch.cuda.Stream()
+    for _ in range(max(args.warmup, 3)):
+        ctx.check(plan.exec(stream))
+    torch.cuda.synchronize()
+    launches0 = binding.launch_count()
+    secs = timed_steps(torch, stream, lambda: ctx.check(plan.exec(stream)), args.steps)
+    launches = binding.launch_count() - launches0
+    value = args.steps * plan.bytes / secs / 1e9
+    tps = args.steps * len(jobs) / secs
+    # the plain path: one blocking drop-in call per transform (device pointers)
+    tmp = torch.empty((1 << 15) + 1, dtype=torch.complex64, device="cuda")
+    def per_call():
+        for kind, n, _, x, y in jobs:
+            if kind == "cfwd":
+                ctx.complex_forward(n, x, y)
+            elif kind == "cinv":
+                ctx.complex_inverse(n, x, y)
+            elif kind == "rfwd":
+                ctx.real_forward(n, x, y)
+            else:
+                ctx.real_inverse(n, x, y, tmp)
+    per_call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    per_call()
+    torch.cuda.synchronize()
+    pc = time.perf_counter() - t0
+    peak, src = measured_peaks()
+    line = base_line(args, "uneven batch FFT GB/s (10000 transforms, log2 n 6..16, mixed kinds)", value, "GB/s", secs,
+                     {"workload": "10000 transforms, log2 n uniform 6..16, 70% complex / 30% real, 50% inverse, "
+                                  "U[-1,1) inputs, one CUDA-graph replay of the persistent job kernel per step",
+                      "jobs": len(jobs), "l2": f"{plan.bytes / 1e9:.2f} GB of algorithmic traffic per step (larger than L2)"})
+    line["transforms_per_s"] = round(tps, 1)
+    line["roofline"] = {"bound": "hbm", "kernel": "k_jobs (persistent job kernel)", "achieved": round(value, 1),
+                        "peak": peak, "unit": "GB/s", "frac": round(value / peak, 4), "peak_source": src,
+                        "traffic": None, "note": "multi-pass jobs (2^14..2^16) move 2x their algorithmic bytes"}
+    line["per_call"] = {"transforms_per_s": round(len(jobs) / pc, 1), "gbs": round(plan.bytes / pc / 1e9, 2),
+                        "api": "one CkFftComplex*/CkFftReal* call per transform (device pointers, blocking)",
+                        "speedup_of_persistent": round(tps / (len(jobs) / pc), 1)}
+    line["gpu_launches"] = launches
+    print(json.dumps(line), flush=True)
+    plan.close()
+    ctx.close()
+
+
 def main():
     args = parse_args()
+    if args.workload != "w2" and args.impl == "ours":
+        {"w1": run_w1, "w3": run_w3, "w4": run_w4, "w5": lambda a: run_w5(a)}[args.workload](args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -304,12 +304,12 @@ int run(CkFftContext* c, const Work& w, const void* in, void* out, cudaStream_t 
     if (!classify(in, c->device, &min) || !classify(out, c->device, &mout)) return 0;
 
     if (user_stream && min == Mem::Device && mout == Mem::Device) {
-        // asynchronous path: scratch from the stream-ordered allocator
+        // asynchronous path: scratch from the library's stream-ordered pool
         const size_t need = scratch_need(w, w.count);
         void* scratch = nullptr;
         if (need) {
-            cudaError_t e = cudaMallocAsync(&scratch, need, user_stream);
-            if (e != cudaSuccess) return cuda_fail("cudaMallocAsync(scratch)", e);
+            cudaError_t e = ckg::pool_alloc_async(&scratch, need, user_stream);
+            if (e != cudaSuccess) return cuda_fail("stream-ordered scratch allocation", e);
         }
         cudaError_t e = enqueue(c, w, w.count, in, out, scratch, need, user_stream);
         if (scratch) cudaFreeAsync(scratch, user_stream);

@@ -70,6 +70,39 @@ unsigned take_device_error()
     return v;
 }
 
+static cudaMemPool_t g_pool[64] = {};
+
+static cudaError_t prepare_pool(int dev)
+{
+    std::lock_guard<std::mutex> lock(g_err_mu);
+    if (dev < 0 || dev >= 64 || g_pool[dev]) return cudaSuccess;
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    cudaError_t e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess) return e;
+    unsigned long long keep = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+        cudaMemPoolDestroy(pool);
+        return e;
+    }
+    g_pool[dev] = pool;
+    return cudaSuccess;
+}
+
+cudaError_t pool_alloc_async(void** p, size_t bytes, cudaStream_t s)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64 || !g_pool[dev]) return cudaMallocAsync(p, bytes, s);
+    return cudaMallocFromPoolAsync(p, bytes, g_pool[dev], s);
+}
+
 static cudaError_t prepare_error_word(int dev)
 {
     std::lock_guard<std::mutex> lock(g_err_mu);
@@ -99,6 +132,7 @@ cudaError_t prepare_device()
     std::lock_guard<std::mutex> lock(mu);
     if (dev < 64 && (done >> dev) & 1ull) return cudaSuccess;
     if ((e = prepare_error_word(dev)) != cudaSuccess) return e;
+    if ((e = prepare_pool(dev)) != cudaSuccess) return e;
     if ((e = prepare_small_c2c()) != cudaSuccess) return e;
     if ((e = prepare_small_real()) != cudaSuccess) return e;
     if ((e = prepare_large()) != cudaSuccess) return e;

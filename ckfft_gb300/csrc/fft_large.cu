@@ -20,28 +20,39 @@ namespace ckg {
 
 // ------------------------------------------------------------ pass kernels
 
+// Thread budget of the batched pass kernels: 1024 for sub-lengths above 2^10
+// (16 values per thread, 64 registers), 512 below.
+template <int LS>
+struct BatchMaxT {
+    static constexpr int value = LS > 10 ? 1024 : 512;
+};
+template <int LS>
+using BPass = PassCfg<LS, BatchMaxT<LS>::value>;
+
 template <int LA, bool INV>
-__global__ void __launch_bounds__(PassCfg<LA>::THREADS)
+__global__ void __launch_bounds__(BPass<LA>::THREADS)
 k_cols(const float2* __restrict__ in, float2* __restrict__ out, long long count, int log2n2,
        long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
-    using P = PassCfg<LA>;
+    using P = BPass<LA>;
     extern __shared__ float2 smem[];
     const long long tiles = (1ll << log2n2) / P::C;
     const long long f = blockIdx.x / tiles;
-    pass_cols<LA, INV, false>(in + f * in_dist, out + f * out_dist, log2n2, blockIdx.x % tiles, threadIdx.x, smem, tw);
+    pass_cols<LA, INV, false, BatchMaxT<LA>::value>(in + f * in_dist, out + f * out_dist, log2n2, blockIdx.x % tiles,
+                                                    threadIdx.x, smem, tw);
 }
 
 template <int LB, bool INV>
-__global__ void __launch_bounds__(PassCfg<LB>::THREADS)
+__global__ void __launch_bounds__(BPass<LB>::THREADS)
 k_rows(const float2* __restrict__ in, float2* __restrict__ out, long long count, int log2n1,
        long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
-    using P = PassCfg<LB>;
+    using P = BPass<LB>;
     extern __shared__ float2 smem[];
     const long long tiles = (1ll << log2n1) / P::C;
     const long long f = blockIdx.x / tiles;
-    pass_rows<LB, INV, false>(in + f * in_dist, out + f * out_dist, log2n1, blockIdx.x % tiles, threadIdx.x, smem, tw);
+    pass_rows<LB, INV, false, BatchMaxT<LB>::value>(in + f * in_dist, out + f * out_dist, log2n1, blockIdx.x % tiles,
+                                                    threadIdx.x, smem, tw);
 }
 
 // ------------------------------------------------- real split / merge passes
@@ -76,7 +87,7 @@ template <int LA, bool INV>
 static cudaError_t launch_cols_L(const float2* in, float2* out, long long count, int log2n2,
                                  long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
 {
-    using P = PassCfg<LA>;
+    using P = BPass<LA>;
     const long long blocks = count * ((1ll << log2n2) / P::C);
     k_cols<LA, INV><<<(unsigned)blocks, P::THREADS, P::SMEM, s>>>(in, out, count, log2n2, in_dist, out_dist, tw);
     return cudaGetLastError();
@@ -86,7 +97,7 @@ template <int LB, bool INV>
 static cudaError_t launch_rows_L(const float2* in, float2* out, long long count, int log2n1,
                                  long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
 {
-    using P = PassCfg<LB>;
+    using P = BPass<LB>;
     const long long blocks = count * ((1ll << log2n1) / P::C);
     k_rows<LB, INV><<<(unsigned)blocks, P::THREADS, P::SMEM, s>>>(in, out, count, log2n1, in_dist, out_dist, tw);
     return cudaGetLastError();
@@ -209,7 +220,7 @@ cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long cou
 template <int L>
 static cudaError_t attr_pass()
 {
-    using P = PassCfg<L>;
+    using P = BPass<L>;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_cols<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(k_cols<L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;

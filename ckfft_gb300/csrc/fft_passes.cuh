@@ -17,13 +17,16 @@ namespace ckg {
 
 // Shape of a sub-transform of 2^LS points inside a pass: R values per thread,
 // C sequences per tile.
-template <int LS>
+// MAXT: thread budget of the CTA (or CTA subgroup) running the tile.  With
+// 512 threads, sub-lengths above 2^10 take 32 values per thread (128
+// registers); with 1024 threads they keep 16 values (64 registers) and twice
+// the resident warps.
+template <int LS, int MAXT = 512>
 struct PassCfg {
-    static constexpr int LOG2R = LS < 4 ? LS : LS <= 10 ? 4 : 5;
+    static constexpr int LOG2R = LS < 4 ? LS : (LS <= 10 || MAXT >= 1024) ? 4 : 5;
     static constexpr int R = 1 << LOG2R;
     static constexpr int T = (1 << LS) / R;
-    // at most 512 threads (so up to 128 registers) and ~140 KB of shared memory
-    static constexpr int C = 512 / T < 16 ? 512 / T : 16;
+    static constexpr int C = MAXT / T < 16 ? MAXT / T : 16;
     static constexpr int THREADS = C * T;
     // interleaved (pass 1 and pass-2 transpose) and per-row padded (pass 2) layouts
     static constexpr int INTERLEAVED = (1 << LS) * C + ((1 << LS) * C >> 4) + 1;
@@ -64,11 +67,11 @@ __device__ __forceinline__ float2 big_twiddle(const float2* __restrict__ tw, int
 }
 
 // Column pass for tile `tile` of one transform, by threads tid = 0..THREADS-1.
-template <int LA, bool INV, bool CG>
+template <int LA, bool INV, bool CG, int MAXT = 512>
 __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
                                           long long tile, int tid, float2* smem, const float2* __restrict__ tw)
 {
-    using P = PassCfg<LA>;
+    using P = PassCfg<LA, MAXT>;
     const int c = tid % P::C, t = tid / P::C;
     const long long n2len = 1ll << log2n2;
     const long long n2 = tile * P::C + c;
@@ -81,22 +84,38 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
     const int ln = LA + log2n2;
     float2* dst = out + n2 + (long long)t * n2len;
     const long long step = (long long)P::T * n2len;
+    // W_N^(n2 k1) for k1 = t + m T, m = 4q + r:  W^(n2 t) * W^(4 n2 T q) * W^(n2 T r).
+    // 3 + log2(R/4) table lookups per thread instead of R; each twiddle is a
+    // product of at most 2 + log2(R/4) rounded factors.
+    const int mask = (1 << ln) - 1;
+    const int p0 = (int)n2 * t, pT = ((int)n2 * P::T) & mask;
+    const float2 a = big_twiddle<INV>(tw, ln, p0 & mask);
+    const float2 b1 = big_twiddle<INV>(tw, ln, pT), b2 = big_twiddle<INV>(tw, ln, (2 * pT) & mask);
+    const float2 b3 = cmul(b1, b2);
+    constexpr int Q = P::R / 4;
+    float2 ladder[Q > 1 ? ilog2(Q) : 1];
 #pragma unroll
-    for (int m = 0; m < P::R; ++m) {
-        const int k1 = t + m * P::T;
-        __stcs(dst + m * step, cmul(v[m], big_twiddle<INV>(tw, ln, (int)n2 * k1)));
-        // keep the compiler from hoisting every twiddle load ahead of the
-        // stores (that would need 4 more registers per value)
-        if ((m & 3) == 3) asm volatile("" ::: "memory");
-    }
+    for (int i = 0; (1 << i) < Q; ++i) ladder[i] = big_twiddle<INV>(tw, ln, (int)(((long long)pT << (2 + i)) & mask));
+    static_for<0, Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        float2 aq = a;
+        static_for<0, (Q > 1 ? ilog2(Q) : 0)>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            if constexpr ((q >> i) & 1) aq = cmul(aq, ladder[i]);
+        });
+        __stcs(dst + (4 * q + 0) * step, cmul(v[4 * q + 0], aq));
+        __stcs(dst + (4 * q + 1) * step, cmul(v[4 * q + 1], cmul(aq, b1)));
+        __stcs(dst + (4 * q + 2) * step, cmul(v[4 * q + 2], cmul(aq, b2)));
+        __stcs(dst + (4 * q + 3) * step, cmul(v[4 * q + 3], cmul(aq, b3)));
+    });
 }
 
 // Row pass for tile `tile` (rows tile*C .. tile*C+C-1) of one transform.
-template <int LB, bool INV, bool CG>
+template <int LB, bool INV, bool CG, int MAXT = 512>
 __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
                                           long long tile, int tid, float2* smem, const float2* __restrict__ tw)
 {
-    using P = PassCfg<LB>;
+    using P = PassCfg<LB, MAXT>;
     constexpr int N2 = 1 << LB;
     const int r = tid / P::T, t = tid % P::T;
     const long long n1len = 1ll << log2n1;

@@ -5,6 +5,7 @@
 // "reset counters + persistent launch" into a CUDA graph, so a replay costs one
 // graph launch regardless of how many transforms the run holds.
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <map>
 #include <new>
@@ -104,7 +105,7 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
         return false;
     }
     std::map<std::pair<int, int>, std::vector<FrameDesc>> buckets;   // (op, log2a) -> frames
-    std::vector<std::vector<Unit>> phase(3);
+    std::vector<std::array<std::vector<Unit>, 3>> phases;           // per multi-pass transform
     for (int j = 0; j < njobs; ++j) {
         const CkFftCudaJob& J = jobs[j];
         char msg[200];
@@ -171,6 +172,8 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
                 // multi-pass transform: phases of column / row tiles (+ merge or split)
                 const int job = (int)b->large.size();
                 b->large.push_back({in, out, nullptr, 0});
+                phases.emplace_back();
+                auto& phase = phases.back();
                 b->scratch_off.push_back(b->scratch_elems);
                 b->scratch_elems += 1ll << lc;
                 const int la = lc / 2, lb = lc - la;
@@ -209,9 +212,8 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
             }
         }
     }
-    // queue: first phase of every multi-pass transform, then the single-CTA
-    // units (largest frames first), then the later phases in order
-    b->units = phase[0];
+    // Single-CTA units, largest frames first.
+    std::vector<Unit> singles;
     std::vector<std::pair<std::pair<int, int>, std::vector<FrameDesc>>> order(buckets.begin(), buckets.end());
     std::stable_sort(order.begin(), order.end(), [](const auto& x, const auto& y) { return x.first.second > y.first.second; });
     for (auto& kv : order) {
@@ -220,12 +222,60 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
         const std::vector<FrameDesc>& fr = kv.second;
         for (size_t i = 0; i < fr.size(); i += per) {
             const int cnt = (int)std::min<size_t>(per, fr.size() - i);
-            b->units.push_back({op, l2, 0, -1, 0, (int)b->frames.size(), cnt, 0});
+            singles.push_back({op, l2, 0, -1, 0, (int)b->frames.size(), cnt, 0});
             b->frames.insert(b->frames.end(), fr.begin() + i, fr.begin() + i + cnt);
         }
     }
-    b->units.insert(b->units.end(), phase[1].begin(), phase[1].end());
-    b->units.insert(b->units.end(), phase[2].begin(), phase[2].end());
+    // Queue order.  The first phase of the multi-pass transforms is spread
+    // over the single-CTA units; each later phase of a transform is placed
+    // `window` units after the last unit of its previous phase.  The window
+    // (twice the resident CTAs) is long enough that the previous phase has
+    // usually finished when the next one is taken (no idle wait), and short
+    // enough that the intermediate it wrote is still in L2.  Phase p of a
+    // transform always follows all of its phase p-1, so every wait is for
+    // units that running CTAs already hold.
+    const size_t window = 2 * (size_t)jobs_grid();
+    struct Pending {
+        size_t ready;
+        int job, phase;
+    };
+    std::vector<Pending> pending;       // kept sorted by `ready`
+    auto push_phase = [&](int job, int p) {
+        b->units.insert(b->units.end(), phases[job][p].begin(), phases[job][p].end());
+        if (p + 1 < 3 && !phases[job][p + 1].empty()) {
+            Pending q{b->units.size() + window, job, p + 1};
+            auto it = std::upper_bound(pending.begin(), pending.end(), q,
+                                       [](const Pending& x, const Pending& y) { return x.ready < y.ready; });
+            pending.insert(it, q);
+        }
+    };
+    auto drain_ready = [&]() {
+        while (!pending.empty() && pending.front().ready <= b->units.size()) {
+            const Pending q = pending.front();
+            pending.erase(pending.begin());
+            push_phase(q.job, q.phase);
+        }
+    };
+    const size_t nl = phases.size();
+    size_t si = 0;
+    for (size_t j = 0; j < nl; ++j) {
+        push_phase((int)j, 0);
+        drain_ready();
+        const size_t upto = singles.size() * (j + 1) / nl;
+        for (; si < upto; ++si) {
+            b->units.push_back(singles[si]);
+            drain_ready();
+        }
+    }
+    for (; si < singles.size(); ++si) {
+        b->units.push_back(singles[si]);
+        drain_ready();
+    }
+    while (!pending.empty()) {
+        const Pending q = pending.front();
+        pending.erase(pending.begin());
+        push_phase(q.job, q.phase);
+    }
     return true;
 }
 
@@ -267,11 +317,11 @@ cudaError_t upload(const Built& b, ContextView cv, void** dmem, float2** scratch
     off = (off + 15) / 16 * 16;
     const size_t o_done = off; off += sizeof(int) * (b.large.size() + 1);   // + queue head
     const size_t total = off + 16;
-    cudaError_t e = async_alloc ? cudaMallocAsync(dmem, total, s) : cudaMalloc(dmem, total);
+    cudaError_t e = async_alloc ? pool_alloc_async(dmem, total, s) : cudaMalloc(dmem, total);
     if (e != cudaSuccess) return e;
     *scratch = nullptr;
     if (b.scratch_elems) {
-        e = async_alloc ? cudaMallocAsync((void**)scratch, sizeof(float2) * b.scratch_elems, s)
+        e = async_alloc ? pool_alloc_async((void**)scratch, sizeof(float2) * b.scratch_elems, s)
                         : cudaMalloc((void**)scratch, sizeof(float2) * b.scratch_elems);
         if (e != cudaSuccess) return e;
     }

@@ -72,4 +72,9 @@ int variant_for(Kind kind, int log2c);
 unsigned* device_error_word();
 unsigned take_device_error();
 
+// Stream-ordered allocation from a library-owned memory pool on the current
+// device; the pool keeps freed memory (release threshold: unlimited), so
+// repeated calls do not map and unmap device memory.  Free with cudaFreeAsync.
+cudaError_t pool_alloc_async(void** p, size_t bytes, cudaStream_t s);
+
 }  // namespace ckg
