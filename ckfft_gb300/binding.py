@@ -77,6 +77,19 @@ def _declare_extras(lib):
     if hasattr(lib, "CkFftCudaComplexBatchNoAlloc"):
         lib.CkFftCudaComplexBatchNoAlloc.restype = i
         lib.CkFftCudaComplexBatchNoAlloc.argtypes = [vp, i, i, i, vp, vp, vp]
+    if hasattr(lib, "CkFftCudaServerCreate"):
+        lib.CkFftCudaServerCreate.restype = vp
+        lib.CkFftCudaServerCreate.argtypes = [vp, C.c_size_t, i]
+        lib.CkFftCudaServerDestroy.restype = None
+        lib.CkFftCudaServerDestroy.argtypes = [vp]
+        lib.CkFftCudaServerSubmit.restype = ll
+        lib.CkFftCudaServerSubmit.argtypes = [vp, vp]
+        lib.CkFftCudaServerWait.restype = i
+        lib.CkFftCudaServerWait.argtypes = [vp, ll, C.c_double, C.POINTER(C.c_double)]
+        lib.CkFftCudaServerReplay.restype = i
+        lib.CkFftCudaServerReplay.argtypes = [vp, vp, i, vp, vp]
+        lib.CkFftCudaReplayPerRequest.restype = i
+        lib.CkFftCudaReplayPerRequest.argtypes = [vp, vp, i, vp, vp]
     if hasattr(lib, "CkFftCudaRunJobs"):
         lib.CkFftCudaRunJobs.restype = i
         lib.CkFftCudaRunJobs.argtypes = [vp, vp, i, vp]
@@ -106,6 +119,19 @@ def job_array(jobs):
     for i, (kind, n, count, inp, out) in enumerate(jobs):
         arr[i] = Job(KIND.get(kind, kind), n, count, ptr(inp), ptr(out))
     return arr, len(jobs)
+
+
+class Request(C.Structure):
+    """CkFftCudaRequest: a job and its arrival time (seconds after the replay starts)."""
+    _fields_ = [("arrival_s", C.c_double), ("job", Job)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("requests", C.c_longlong), ("seconds", C.c_double), ("algo_bytes", C.c_double),
+                ("p50_s", C.c_double), ("p99_s", C.c_double), ("p999_s", C.c_double), ("max_s", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 def last_error() -> str:
@@ -219,3 +245,55 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """CkFftCudaServer: continuous-batching request server on one context."""
+
+    def __init__(self, ctx: Context, scratch_budget_bytes: int = 2 << 30, max_inflight: int = 3):
+        self.lib = ctx.lib
+        self.ctx = ctx
+        self.handle = self.lib.CkFftCudaServerCreate(ctx.handle, scratch_budget_bytes, max_inflight)
+        if not self.handle:
+            raise CkFftError(f"CkFftCudaServerCreate failed: {last_error()}")
+
+    def submit(self, kind, n, count, inp, out) -> int:
+        job = Job(KIND.get(kind, kind), n, count, ptr(inp), ptr(out))
+        return self.lib.CkFftCudaServerSubmit(self.handle, C.byref(job))
+
+    def wait(self, ticket: int, timeout_s: float = -1.0):
+        lat = C.c_double(0.0)
+        ok = self.lib.CkFftCudaServerWait(self.handle, ticket, timeout_s, C.byref(lat))
+        return ok, lat.value
+
+    def replay(self, requests):
+        """requests: list of (arrival_s, kind, n, count, input, output)."""
+        arr, lat, st = _requests(requests)
+        ok = self.lib.CkFftCudaServerReplay(self.handle, C.cast(arr, C.c_void_p), len(requests), lat, C.byref(st))
+        return ok, list(lat), st.as_dict()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.CkFftCudaServerDestroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _requests(requests):
+    arr = (Request * max(1, len(requests)))()
+    for i, (t, kind, n, count, inp, out) in enumerate(requests):
+        arr[i] = Request(t, Job(KIND.get(kind, kind), n, count, ptr(inp), ptr(out)))
+    lat = (C.c_double * max(1, len(requests)))()
+    return arr, lat, ServeStats()
+
+
+def replay_per_request(ctx: Context, requests):
+    """The same trace through one blocking batch call per request."""
+    arr, lat, st = _requests(requests)
+    ok = ctx.lib.CkFftCudaReplayPerRequest(ctx.handle, C.cast(arr, C.c_void_p), len(requests), lat, C.byref(st))
+    return ok, list(lat), st.as_dict()

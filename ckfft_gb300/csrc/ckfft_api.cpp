@@ -416,13 +416,6 @@ int complex_call(CkFftContext* c, bool inverse, int n, long long count, const Ck
 
 namespace ckg {
 
-// Read-only view of a context for entry points defined in other files.
-struct ContextView {
-    int nmax;
-    int direction;
-    int device;
-    const float2* tw;
-};
 
 bool context_view(const CkFftContext* c, ContextView* out)
 {

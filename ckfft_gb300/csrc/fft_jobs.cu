@@ -195,19 +195,29 @@ __global__ void __launch_bounds__(kJobThreads, 2) k_jobs(JobsArgs a)
     extern __shared__ __align__(128) float2 smem[];
     __shared__ int s_unit;
     __shared__ int s_ok;
+    // The next unit is claimed when the current one starts, so the atomic's
+    // round trip overlaps the work.  Still deadlock-free: the lowest-indexed
+    // unit in progress depends only on lower indices, all of which are done.
+    if (threadIdx.x == 0) s_unit = atomicAdd(a.head, 1);
     for (;;) {
-        if (threadIdx.x == 0) s_unit = atomicAdd(a.head, 1);
         __syncthreads();
         const int ui = s_unit;
         if (ui >= a.nunits) break;
         const Unit u = a.units[ui];
-        if (threadIdx.x == 0) s_ok = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err) : 1;
+        int next = 0;
+        if (threadIdx.x == 0) {
+            next = atomicAdd(a.head, 1);
+            s_ok = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err) : 1;
+        }
         __syncthreads();
         if (s_ok) dispatch(u, a, smem);
         __syncthreads();
-        if (u.job >= 0 && threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(a.done + u.job, 1);
+        if (threadIdx.x == 0) {
+            if (u.job >= 0) {
+                __threadfence();
+                atomicAdd(a.done + u.job, 1);
+            }
+            s_unit = next;
         }
     }
 }

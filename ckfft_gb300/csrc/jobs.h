@@ -14,6 +14,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "ckfft_cuda.h"
+
 namespace ckg {
 
 enum UnitOp : int {
@@ -74,6 +76,29 @@ constexpr int kJobThreads = 512;
 constexpr int kJobMaxLog2Complex = 20;
 // Single-CTA sizes inside the job kernel (complex length, 64 registers).
 constexpr int kJobMaxSingleLog2 = 13;
+
+struct ContextView;
+
+// Resident buffers of one in-flight run (grown on demand and reused; a slot
+// may be refilled only after its previous run has completed).
+struct RunSlot {
+    void* dev = nullptr;         // units | frames | large | counters, device
+    size_t dev_cap = 0;
+    char* host = nullptr;        // the same, pinned staging on the host
+    size_t host_cap = 0;
+    float2* scratch = nullptr;   // multi-pass intermediates
+    size_t scratch_cap = 0;
+};
+void free_run_slot(RunSlot* r);
+// Validates, builds and enqueues a mixed run on `s` with the slot's buffers.
+// 1 on success, 0 on invalid jobs, -1 on a CUDA failure (message set).
+// scratch_override: caller-owned intermediates (>= the run's scratch bytes);
+// NULL uses (and grows) the slot's own scratch.
+int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunSlot* r, cudaStream_t s,
+                float2* scratch_override = nullptr);
+bool validate_job(const ContextView& cv, const CkFftCudaJob& j, int index);
+long long job_scratch_bytes(const CkFftCudaJob& j);
+long long job_algo_bytes(const CkFftCudaJob& j);
 
 // Launches the job kernel on all resident CTAs of the current device.
 cudaError_t launch_jobs(const JobsArgs& a, cudaStream_t s);

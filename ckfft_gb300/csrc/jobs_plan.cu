@@ -20,14 +20,6 @@
 
 namespace ckg {
 
-struct ContextView {
-    int nmax;
-    int direction;
-    int device;
-    const float2* tw;
-};
-bool context_view(const CkFftContext* c, ContextView* out);
-void set_last_error(const char* msg);
 
 // Threads per tile and tiles per pass unit for sub-length 2^LS (PassCfg).
 struct PassShape {
@@ -97,6 +89,58 @@ static bool on_device(const void* p, int dev)
     return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
+// Checks one job against the rules of the single calls plus the job
+// kernel's limits; sets the error message (naming job `j`) on failure.
+bool validate_job(const ContextView& cv, const CkFftCudaJob& J, int j)
+{
+    char msg[200];
+    if (J.kind < 0 || J.kind > 3) {
+        snprintf(msg, sizeof msg, "job %d: kind must be 0..3", j);
+        set_last_error(msg);
+        return false;
+    }
+    const bool inverse = J.kind == 1 || J.kind == 3;
+    const bool real = J.kind >= 2;
+    if (!(cv.direction & (inverse ? kCkFftDirection_Inverse : kCkFftDirection_Forward))) {
+        snprintf(msg, sizeof msg, "job %d: context was created without this direction", j);
+        set_last_error(msg);
+        return false;
+    }
+    if (J.n <= 0 || (J.n & (J.n - 1)) || J.n > cv.nmax) {
+        snprintf(msg, sizeof msg, "job %d: n must be a power of two no larger than the context's nMax", j);
+        set_last_error(msg);
+        return false;
+    }
+    if (J.count < 0) {
+        snprintf(msg, sizeof msg, "job %d: count must be >= 0", j);
+        set_last_error(msg);
+        return false;
+    }
+    if (J.count == 0) return true;
+    if (!J.input || !J.output || J.input == J.output) {
+        snprintf(msg, sizeof msg, "job %d: input and output must be distinct non-NULL buffers", j);
+        set_last_error(msg);
+        return false;
+    }
+    if (!on_device(J.input, cv.device) || !on_device(J.output, cv.device)) {
+        snprintf(msg, sizeof msg, "job %d: jobs take device (or managed) memory", j);
+        set_last_error(msg);
+        return false;
+    }
+    if (((uintptr_t)J.input & 7) || ((uintptr_t)J.output & 7)) {
+        snprintf(msg, sizeof msg, "job %d: device buffers must be 8-byte aligned", j);
+        set_last_error(msg);
+        return false;
+    }
+    const int lc = ilog2ll(J.n) - (real ? 1 : 0);
+    if (lc > kJobMaxLog2Complex) {
+        snprintf(msg, sizeof msg, "job %d: n = %d exceeds the job kernel's limit (complex 2^20, real 2^21)", j, J.n);
+        set_last_error(msg);
+        return false;
+    }
+    return true;
+}
+
 // Validates the jobs and builds the unit queue.  Returns false with an error set.
 static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, Built* b)
 {
@@ -108,52 +152,12 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
     std::vector<std::array<std::vector<Unit>, 3>> phases;           // per multi-pass transform
     for (int j = 0; j < njobs; ++j) {
         const CkFftCudaJob& J = jobs[j];
-        char msg[200];
-        if (J.kind < 0 || J.kind > 3) {
-            snprintf(msg, sizeof msg, "job %d: kind must be 0..3", j);
-            set_last_error(msg);
-            return false;
-        }
+        if (!validate_job(cv, J, j)) return false;
+        if (J.count == 0) continue;
         const bool inverse = J.kind == 1 || J.kind == 3;
         const bool real = J.kind >= 2;
-        if (!(cv.direction & (inverse ? kCkFftDirection_Inverse : kCkFftDirection_Forward))) {
-            snprintf(msg, sizeof msg, "job %d: context was created without this direction", j);
-            set_last_error(msg);
-            return false;
-        }
-        if (J.n <= 0 || (J.n & (J.n - 1)) || J.n > cv.nmax) {
-            snprintf(msg, sizeof msg, "job %d: n must be a power of two no larger than the context's nMax", j);
-            set_last_error(msg);
-            return false;
-        }
-        if (J.count < 0) {
-            snprintf(msg, sizeof msg, "job %d: count must be >= 0", j);
-            set_last_error(msg);
-            return false;
-        }
-        if (J.count == 0) continue;
-        if (!J.input || !J.output || J.input == J.output) {
-            snprintf(msg, sizeof msg, "job %d: input and output must be distinct non-NULL buffers", j);
-            set_last_error(msg);
-            return false;
-        }
-        if (!on_device(J.input, cv.device) || !on_device(J.output, cv.device)) {
-            snprintf(msg, sizeof msg, "job %d: jobs take device (or managed) memory", j);
-            set_last_error(msg);
-            return false;
-        }
-        if (((uintptr_t)J.input & 7) || ((uintptr_t)J.output & 7)) {
-            snprintf(msg, sizeof msg, "job %d: device buffers must be 8-byte aligned", j);
-            set_last_error(msg);
-            return false;
-        }
         const int L = ilog2ll(J.n);
         const int lc = real ? L - 1 : L;                     // complex (half-)length
-        if (lc > kJobMaxLog2Complex) {
-            snprintf(msg, sizeof msg, "job %d: n = %d exceeds the job kernel's limit (complex 2^20, real 2^21)", j, J.n);
-            set_last_error(msg);
-            return false;
-        }
         const long long in_dist = real ? (inverse ? J.n / 2 + 1 : J.n / 2) : J.n;    // float2 units
         const long long out_dist = real ? (inverse ? J.n / 2 : J.n / 2 + 1) : J.n;
         const long long in_stride_bytes = real && !inverse ? 4ll * J.n : 8ll * in_dist;
@@ -277,6 +281,102 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
         push_phase(q.job, q.phase);
     }
     return true;
+}
+
+// Scratch bytes one job needs in a run (multi-pass intermediates; 0 for
+// single-CTA sizes).
+long long job_scratch_bytes(const CkFftCudaJob& j)
+{
+    if (j.count <= 0 || j.n <= 0) return 0;
+    const bool real = j.kind >= 2;
+    const int lc = ilog2ll(j.n) - (real ? 1 : 0);
+    if ((real && j.n <= 4) || lc <= kJobMaxSingleLog2) return 0;
+    return (long long)j.count * (long long)sizeof(float2) * (1ll << lc);
+}
+
+long long job_algo_bytes(const CkFftCudaJob& j)
+{
+    const bool real = j.kind >= 2;
+    return (long long)j.count * (real ? 4ll * j.n + 8ll * (j.n / 2 + 1) : 16ll * j.n);
+}
+
+void free_run_slot(RunSlot* r)
+{
+    cudaFree(r->dev);
+    cudaFreeHost(r->host);
+    cudaFree(r->scratch);
+    *r = RunSlot{};
+}
+
+static cudaError_t grow_dev(void** p, size_t* cap, size_t need)
+{
+    if (*cap >= need) return cudaSuccess;
+    cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const size_t want = need + need / 4;
+    cudaError_t e = cudaMalloc(p, want);
+    if (e == cudaSuccess) *cap = want;
+    return e;
+}
+
+int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunSlot* r, cudaStream_t s,
+                float2* scratch_override)
+{
+    Built b;
+    if (!build_units(cv, jobs, njobs, &b)) return 0;
+    if (b.units.empty()) return 1;
+    size_t off = 0;
+    const size_t o_units = off; off += sizeof(Unit) * b.units.size();
+    off = (off + 15) / 16 * 16;
+    const size_t o_frames = off; off += sizeof(FrameDesc) * b.frames.size();
+    off = (off + 15) / 16 * 16;
+    const size_t o_large = off; off += sizeof(LargeDesc) * b.large.size();
+    off = (off + 15) / 16 * 16;
+    const size_t o_done = off; off += sizeof(int) * (b.large.size() + 1);
+    const size_t total = off + 16;
+    cudaError_t e = cudaSuccess;
+    if (r->host_cap < total) {
+        cudaFreeHost(r->host);
+        r->host = nullptr;
+        r->host_cap = 0;
+        e = cudaHostAlloc((void**)&r->host, total + total / 4, cudaHostAllocDefault);
+        if (e == cudaSuccess) r->host_cap = total + total / 4;
+    }
+    if (e == cudaSuccess) e = grow_dev(&r->dev, &r->dev_cap, total);
+    if (e == cudaSuccess && b.scratch_elems && !scratch_override)
+        e = grow_dev((void**)&r->scratch, &r->scratch_cap, sizeof(float2) * (size_t)b.scratch_elems);
+    float2* scratch = scratch_override ? scratch_override : r->scratch;
+    if (e != cudaSuccess) {
+        set_last_error(cudaGetErrorString(e));
+        return -1;
+    }
+    memcpy(r->host + o_units, b.units.data(), sizeof(Unit) * b.units.size());
+    memcpy(r->host + o_frames, b.frames.data(), sizeof(FrameDesc) * b.frames.size());
+    LargeDesc* ld = (LargeDesc*)(r->host + o_large);
+    for (size_t i = 0; i < b.large.size(); ++i) {
+        ld[i] = b.large[i];
+        ld[i].scratch = scratch + b.scratch_off[i];
+    }
+    memset(r->host + o_done, 0, sizeof(int) * (b.large.size() + 1));
+    char* base = (char*)r->dev;
+    JobsArgs a{};
+    a.units = (const Unit*)(base + o_units);
+    a.nunits = (int)b.units.size();
+    a.frames = (const FrameDesc*)(base + o_frames);
+    a.large = (const LargeDesc*)(base + o_large);
+    a.done = (int*)(base + o_done);
+    a.head = a.done + b.large.size();
+    a.tw = cv.tw;
+    a.err = device_error_word();
+    e = cudaMemcpyAsync(r->dev, r->host, total, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_jobs(a, s);
+    if (e != cudaSuccess) {
+        set_last_error(cudaGetErrorString(e));
+        return -1;
+    }
+    count_launch();
+    return 1;
 }
 
 }  // namespace ckg

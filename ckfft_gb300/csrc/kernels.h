@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 
+struct _CkFftContext;
+
 namespace ckg {
 
 enum Kind : int { C2C_FWD = 0, C2C_INV = 1, R2C = 2, C2R = 3 };
@@ -59,6 +61,18 @@ cudaError_t prepare_device();
 // Kernel launches issued so far by this process.
 long long launch_count();
 void count_launch(int n = 1);
+
+// Read-only view of a context for entry points defined outside ckfft_api.cpp.
+struct ContextView {
+    int nmax;
+    int direction;
+    int device;
+    const float2* tw;
+};
+// Validates a context handle and copies its fields (ckfft_api.cpp).
+bool context_view(const struct ::_CkFftContext* c, ContextView* out);
+// Sets the calling thread's CkFftCudaGetLastError() message.
+void set_last_error(const char* msg);
 
 // Smallest log2 (complex) length served by the pipelined persistent kernels.
 constexpr int kPipeMinLog2 = 6;

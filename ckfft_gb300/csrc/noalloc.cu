@@ -29,15 +29,6 @@
 
 namespace ckg {
 
-struct ContextView {
-    int nmax;
-    int direction;
-    int device;
-    const float2* tw;
-};
-// Defined in ckfft_api.cpp: validates the handle and copies its fields.
-bool context_view(const CkFftContext* c, ContextView* out);
-void set_last_error(const char* msg);
 
 constexpr int kNoAllocMaxLog2 = 20;
 constexpr size_t kNoAllocScratchBytes = sizeof(float2) << kNoAllocMaxLog2;   // 8 MiB

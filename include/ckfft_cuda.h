@@ -167,6 +167,63 @@ long long CkFftCudaPlanBytes(const CkFftCudaPlan* plan);
  * stream NULL blocks until done. */
 int CkFftCudaRunJobs(CkFftContext* context, const CkFftCudaJob* jobs, int njobs, void* stream);
 
+/* ----------------------------------------------------------------------
+ * Serving: a request server with continuous batching (no counterpart in the
+ * reference).  A dispatcher thread keeps up to max_inflight runs of the
+ * persistent job kernel on the GPU; requests submitted while runs are in
+ * flight are admitted, in arrival order, into the next free run slot while
+ * their multi-pass scratch fits the slot's share of scratch_budget_bytes (a
+ * larger request runs alone once free HBM covers it).
+ * ---------------------------------------------------------------------- */
+
+typedef struct _CkFftCudaServer CkFftCudaServer;
+
+/* A request of a replayed trace: a job and its arrival time in seconds after
+ * the replay starts. */
+typedef struct
+{
+    double arrival_s;
+    CkFftCudaJob job;
+}
+CkFftCudaRequest;
+
+/* Latency and throughput of a replay.  Latency runs from a request's
+ * scheduled arrival to the moment its results are complete on the device. */
+typedef struct
+{
+    long long requests;
+    double seconds;        /* first arrival to last completion */
+    double algo_bytes;     /* algorithmic bytes of all requests */
+    double p50_s;
+    double p99_s;
+    double p999_s;
+    double max_s;
+}
+CkFftCudaServeStats;
+
+CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_budget_bytes, int max_inflight);
+void CkFftCudaServerDestroy(CkFftCudaServer* server);   /* finishes admitted work first */
+
+/* Queues one request (validated like a job; device buffers).  Returns a ticket
+ * > 0, or 0 on error.  Never blocks on the GPU. */
+long long CkFftCudaServerSubmit(CkFftCudaServer* server, const CkFftCudaJob* job);
+
+/* Waits for a ticket (timeout_s < 0: no limit).  1 when its results are
+ * complete (latency_s: submission to completion), 0 on timeout or failure. */
+int CkFftCudaServerWait(CkFftCudaServer* server, long long ticket, double timeout_s, double* latency_s);
+
+/* Submits a trace at its arrival times from the calling thread, waits for every
+ * request, and reports per-request latency (latency_s[n], may be NULL) and
+ * statistics.  Returns 1 when every request completed. */
+int CkFftCudaServerReplay(CkFftCudaServer* server, const CkFftCudaRequest* requests, int n,
+                          double* latency_s, CkFftCudaServeStats* stats);
+
+/* The same trace through the plain path, one batch call per request at its
+ * arrival (one launch per request, two or three for multi-pass sizes),
+ * blocking: the comparison point for the server. */
+int CkFftCudaReplayPerRequest(CkFftContext* context, const CkFftCudaRequest* requests, int n,
+                              double* latency_s, CkFftCudaServeStats* stats);
+
 /* Complex batch that allocates no memory.  No counterpart in the reference.
  * For callers that must not allocate while they run: a real-time audio
  * callback cannot wait for cudaMalloc/cudaFree (they can synchronise the whole
