@@ -53,6 +53,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-percall", action="store_true")
+    ap.add_argument("--direct-mb", type=int, default=8, help="w5: requests this large skip batching")
     ap.add_argument("--workload", choices=["w1", "w2", "w3", "w4", "w5"], default="w2",
                     help="w2 (default): real n=4096 x 65536 frames; w1: complex n=1024 x 4096 round trip; "
                          "w3: large single complex transforms; w4: uneven mixed batch; w5: serving")
@@ -297,14 +298,8 @@ def run_ours(args, rank, world, local_rank):
     sampler.stop()
     secs = start.elapsed_time(end) / 1e3
     fwd_ms = sum(a.elapsed_time(b) for a, b in fwd_events) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([secs], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs = float(t.item())
-
     bytes_step = frames * 2 * frame_bytes(n)
-    value = world * bytes_step * args.steps / secs / 1e9
+    secs, value = combine_ranks(secs, bytes_step * args.steps, world)
     peak, peak_kind = measured_peaks()
     achieved = frames * frame_bytes(n) / (fwd_ms / 1e3) / 1e9
     traffic = ncu_traffic()
@@ -381,6 +376,20 @@ def measure_per_call(torch, ctx, x, n, calls=512):
     dt = time.perf_counter() - t0
     return {"transforms_per_s": round(calls / dt, 1), "gbs": round(calls * frame_bytes(n) / dt / 1e9, 3),
             "calls": calls, "api": "CkFftRealForward per frame (device pointers, blocking)"}
+
+
+def combine_ranks(secs, bytes_local, world):
+    """Whole-job figures from each rank's timed region: the slowest rank's time
+    (max over ranks, a collective on the timing only) and the bytes of all
+    ranks (every rank processes its own frames: weak scaling)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([secs], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+    return secs, world * bytes_local / secs / 1e9
 
 
 # ------------------------------------------------------------ other workloads
@@ -632,10 +641,83 @@ def run_w4(args):
     ctx.close()
 
 
+def run_w5(args, nreq=600):
+    """Workload 5: Poisson request stream (sizes 2^k, k in 8..20, 1-64 frames,
+    mixed complex/real, N(0,1) inputs) at 10-90% of the server's measured peak,
+    through the continuous-batching server and through one call per request."""
+    import numpy as np
+    import torch
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+
+    rng = np.random.default_rng(wl.W5_SEED)
+    lo, hi = wl.W5_LOG2
+    l2 = rng.integers(lo, hi + 1, nreq)
+    frames = rng.integers(1, 65, nreq)
+    real = rng.uniform(size=nreq) < 0.5
+    inv = rng.uniform(size=nreq) < 0.5
+    kinds = [("rinv" if i else "rfwd") if r else ("cinv" if i else "cfwd") for r, i in zip(real, inv)]
+    ns = [1 << int(k) for k in l2]
+
+    def in_bytes(kind, n, c):
+        return c * (4 * n if kind == "rfwd" else 8 * (n // 2 + 1) if kind == "rinv" else 8 * n)
+
+    def out_bytes(kind, n, c):
+        return c * (8 * (n // 2 + 1) if kind == "rfwd" else 4 * n if kind == "rinv" else 8 * n)
+
+    ctx = binding.Context(1 << hi)
+    max_in = max(in_bytes(k, n, int(c)) for k, n, c in zip(kinds, ns, frames))
+    g = torch.Generator(device="cuda")
+    g.manual_seed(wl.W5_SEED)
+    src = torch.randn(max_in // 4 + 16, generator=g, device="cuda")       # shared, read-only inputs
+    offs = np.cumsum([0] + [(out_bytes(k, n, int(c)) + 255) // 256 * 256 for k, n, c in zip(kinds, ns, frames)])
+    dst = torch.empty(int(offs[-1]) // 4 + 64, device="cuda")              # a distinct output per request
+    base_in, base_out = src.data_ptr(), dst.data_ptr()
+    reqs = [(k, n, int(c), base_in, base_out + int(o)) for k, n, c, o in zip(kinds, ns, frames, offs[:-1])]
+    algo = sum(wl.algorithmic_bytes(k in ("rfwd", "rinv"), n) * int(c) for k, n, c in zip(kinds, ns, frames))
+    mean_bytes = algo / nreq
+
+    srv = binding.Server(ctx, scratch_budget_bytes=4 << 30, max_inflight=2, direct_threshold_bytes=args.direct_mb << 20)
+    burst = [(0.0,) + r for r in reqs]
+    srv.replay(burst)                                                      # warm-up
+    ok, _, st = srv.replay(burst)
+    if not ok:
+        raise SystemExit(f"server replay failed: {binding.last_error()}")
+    peak_gbs = st["algo_bytes"] / st["seconds"] / 1e9
+    loads = []
+    for f in (0.1, 0.3, 0.5, 0.7, 0.9):
+        rate = f * peak_gbs * 1e9 / mean_bytes
+        t = np.cumsum(np.random.default_rng(int(f * 100)).exponential(1.0 / rate, nreq))
+        trace = [(float(ti),) + r for ti, r in zip(t, reqs)]
+        ok1, _, s1 = srv.replay(trace)
+        ok2, _, s2 = binding.replay_per_request(ctx, trace)
+        if not (ok1 and ok2):
+            raise SystemExit(f"replay failed: {binding.last_error()}")
+        row = {"load": f, "offered_req_per_s": round(rate, 1)}
+        for name, sx in (("server", s1), ("per_request", s2)):
+            row[name] = {"p50_ms": round(sx["p50_s"] * 1e3, 4), "p99_ms": round(sx["p99_s"] * 1e3, 4),
+                         "p999_ms": round(sx["p999_s"] * 1e3, 4), "max_ms": round(sx["max_s"] * 1e3, 4),
+                         "throughput_gbs": round(sx["algo_bytes"] / sx["seconds"] / 1e9, 1)}
+        loads.append(row)
+    srv.close()
+    mid = next(r for r in loads if r["load"] == 0.5)
+    line = {"metric": "served p99 latency at 50% of peak offered load", "value": mid["server"]["p99_ms"],
+            "unit": "ms", "n_gpus": 1, "steps": len(loads), "warmup": 1, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded N(0,1) inputs)",
+            "config": {"workload": f"{nreq} requests, size 2^k with k uniform in {lo}..{hi}, 1-64 frames, "
+                                   "50% real / 50% complex, 50% inverse, Poisson arrivals",
+                       "server": f"2 job-kernel runs in flight, requests >= {args.direct_mb} MiB on 2 direct lanes, "
+                                 "4 GiB scratch budget, device-resident inputs and outputs",
+                       "mean_request_mb": round(mean_bytes / 1e6, 2)},
+            "peak_gbs": round(peak_gbs, 1), "loads": loads}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse_args()
     if args.workload != "w2" and args.impl == "ours":
-        {"w1": run_w1, "w3": run_w3, "w4": run_w4, "w5": lambda a: run_w5(a)}[args.workload](args)
+        {"w1": run_w1, "w3": run_w3, "w4": run_w4, "w5": run_w5}[args.workload](args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

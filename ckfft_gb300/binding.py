@@ -79,7 +79,7 @@ def _declare_extras(lib):
         lib.CkFftCudaComplexBatchNoAlloc.argtypes = [vp, i, i, i, vp, vp, vp]
     if hasattr(lib, "CkFftCudaServerCreate"):
         lib.CkFftCudaServerCreate.restype = vp
-        lib.CkFftCudaServerCreate.argtypes = [vp, C.c_size_t, i]
+        lib.CkFftCudaServerCreate.argtypes = [vp, C.c_size_t, i, ll]
         lib.CkFftCudaServerDestroy.restype = None
         lib.CkFftCudaServerDestroy.argtypes = [vp]
         lib.CkFftCudaServerSubmit.restype = ll
@@ -250,10 +250,12 @@ class Plan:
 class Server:
     """CkFftCudaServer: continuous-batching request server on one context."""
 
-    def __init__(self, ctx: Context, scratch_budget_bytes: int = 2 << 30, max_inflight: int = 3):
+    def __init__(self, ctx: Context, scratch_budget_bytes: int = 2 << 30, max_inflight: int = 3,
+                 direct_threshold_bytes: int = 8 << 20):
         self.lib = ctx.lib
         self.ctx = ctx
-        self.handle = self.lib.CkFftCudaServerCreate(ctx.handle, scratch_budget_bytes, max_inflight)
+        self.handle = self.lib.CkFftCudaServerCreate(ctx.handle, scratch_budget_bytes, max_inflight,
+                                                     direct_threshold_bytes)
         if not self.handle:
             raise CkFftError(f"CkFftCudaServerCreate failed: {last_error()}")
 

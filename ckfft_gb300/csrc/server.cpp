@@ -10,9 +10,13 @@
 // HBM (cudaMemGetInfo) covers its scratch, which then comes from the
 // library's stream-ordered pool.  Requests that arrive while earlier runs are
 // still on the GPU therefore start as soon as a slot frees up and their work
-// overlaps the runs already in flight.  Completion is detected by polling each
-// run's event; latency is measured from submission (or scheduled arrival, for
-// trace replays) to the dispatcher observing the run's completion.
+// overlaps the runs already in flight.  Requests whose algorithmic bytes reach
+// `direct_threshold_bytes` already fill the GPU on their own: they skip
+// batching and go to one of two direct lanes (the batched entry points on a
+// lane stream), so a small request never waits behind a large one inside a
+// run.  Completion is detected by polling each run's or lane's event; latency
+// is measured from submission (or scheduled arrival, for trace replays) to
+// the dispatcher observing the completion.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -61,18 +65,32 @@ struct Slot {
     std::vector<Request> reqs;
 };
 
+// A direct lane runs one large request at a time through the batched entry
+// points (one launch, or two or three for multi-pass sizes) on its own stream.
+struct Lane {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev = nullptr;
+    bool busy = false;
+    std::vector<Request> reqs;   // zero or one
+};
+
 constexpr int kMaxRequestsPerRun = 4096;
+constexpr int kDirectLanes = 2;
 
 }  // namespace
 
 struct _CkFftCudaServer {
     ckg::ContextView cv{};
+    CkFftContext* ctx = nullptr;
     size_t arena = 0;
+    long long direct_bytes = 0;     // requests this large skip batching
     std::vector<Slot> slots;
+    std::vector<Lane> lanes;
     std::mutex mu;
     std::condition_variable cv_pending;
     std::condition_variable cv_done;
-    std::deque<Request> pending;
+    std::deque<Request> pending;    // batched
+    std::deque<Request> direct;     // direct lanes
     std::unordered_map<long long, Result> results;
     std::thread dispatcher;
     std::atomic<bool> stop{false};
@@ -91,6 +109,39 @@ struct DevScope {
     }
     ~DevScope() { if (prev >= 0) cudaSetDevice(prev); }
 };
+
+void complete(CkFftCudaServer* s, std::vector<Request>& reqs, bool ok)
+{
+    const Clock::time_point now = Clock::now();
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        for (const Request& r : reqs) {
+            Result& res = s->results[r.ticket];
+            res.done = true;
+            res.ok = ok;
+            res.latency = seconds_between(r.t0, now);
+            s->completed += 1;
+            s->algo_bytes += (double)r.bytes;
+        }
+    }
+    reqs.clear();
+    s->cv_done.notify_all();
+}
+
+// Enqueues a large request through the batched entry points.
+bool enqueue_direct(CkFftCudaServer* s, const CkFftCudaJob& j, cudaStream_t st)
+{
+    switch (j.kind) {
+    case CKFFT_CUDA_COMPLEX_FORWARD:
+        return CkFftCudaComplexForwardBatch(s->ctx, j.n, j.count, (const CkFftComplex*)j.input, (CkFftComplex*)j.output, st);
+    case CKFFT_CUDA_COMPLEX_INVERSE:
+        return CkFftCudaComplexInverseBatch(s->ctx, j.n, j.count, (const CkFftComplex*)j.input, (CkFftComplex*)j.output, st);
+    case CKFFT_CUDA_REAL_FORWARD:
+        return CkFftCudaRealForwardBatch(s->ctx, j.n, j.count, (const float*)j.input, (CkFftComplex*)j.output, st);
+    default:
+        return CkFftCudaRealInverseBatch(s->ctx, j.n, j.count, (const CkFftComplex*)j.input, (float*)j.output, st);
+    }
+}
 
 void finish_slot(CkFftCudaServer* s, Slot& sl, bool ok)
 {
@@ -147,6 +198,35 @@ void dispatch_loop(CkFftCudaServer* s)
     while (true) {
         bool progressed = false;
         int busy = 0;
+        // direct lanes: completions, then the next large request
+        for (Lane& ln : s->lanes) {
+            if (ln.busy) {
+                const cudaError_t q = cudaEventQuery(ln.ev);
+                if (q == cudaErrorNotReady) {
+                    ++busy;
+                    continue;
+                }
+                if (q != cudaSuccess) cudaGetLastError();
+                complete(s, ln.reqs, q == cudaSuccess && ckg::take_device_error() == 0);
+                ln.busy = false;
+                progressed = true;
+            }
+            Request r;
+            {
+                std::lock_guard<std::mutex> lock(s->mu);
+                if (s->direct.empty()) continue;
+                r = s->direct.front();
+                s->direct.pop_front();
+            }
+            ln.reqs.assign(1, r);
+            if (enqueue_direct(s, r.job, ln.stream) && cudaEventRecord(ln.ev, ln.stream) == cudaSuccess) {
+                ln.busy = true;
+                ++busy;
+            } else {
+                complete(s, ln.reqs, false);
+            }
+            progressed = true;
+        }
         for (Slot& sl : s->slots) {
             if (!sl.busy) continue;
             const cudaError_t q = cudaEventQuery(sl.ev);
@@ -196,7 +276,7 @@ void dispatch_loop(CkFftCudaServer* s)
         }
         if (s->stop.load() && busy == 0) {
             std::lock_guard<std::mutex> lock(s->mu);
-            if (s->pending.empty()) break;
+            if (s->pending.empty() && s->direct.empty()) break;
         }
         if (!progressed) {
             if (busy) {
@@ -204,7 +284,7 @@ void dispatch_loop(CkFftCudaServer* s)
             } else {
                 std::unique_lock<std::mutex> lock(s->mu);
                 s->cv_pending.wait_for(lock, std::chrono::milliseconds(1),
-                                       [&] { return !s->pending.empty() || s->stop.load(); });
+                                       [&] { return !s->pending.empty() || !s->direct.empty() || s->stop.load(); });
             }
         }
     }
@@ -222,7 +302,8 @@ long long submit(CkFftCudaServer* s, const CkFftCudaJob& job, Clock::time_point 
         std::lock_guard<std::mutex> lock(s->mu);
         r.ticket = s->next_ticket++;
         s->results[r.ticket] = Result{};
-        s->pending.push_back(r);
+        if (s->direct_bytes > 0 && r.bytes >= s->direct_bytes) s->direct.push_back(r);
+        else s->pending.push_back(r);
     }
     s->cv_pending.notify_one();
     return r.ticket;
@@ -273,7 +354,8 @@ void spin_until(Clock::time_point t)
 
 extern "C" {
 
-CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_budget_bytes, int max_inflight)
+CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_budget_bytes, int max_inflight,
+                                       long long direct_threshold_bytes)
 {
     ckg::ContextView cv;
     if (!ckg::context_view(context, &cv)) { ckg::set_last_error("NULL or invalid context"); return nullptr; }
@@ -282,9 +364,16 @@ CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_bud
     CkFftCudaServer* s = new (std::nothrow) _CkFftCudaServer();
     if (!s) { ckg::set_last_error("out of host memory"); return nullptr; }
     s->cv = cv;
+    s->ctx = context;
     s->arena = scratch_budget_bytes / (size_t)max_inflight / 16 * 16;
+    s->direct_bytes = direct_threshold_bytes;
     s->slots.resize(max_inflight);
+    s->lanes.resize(direct_threshold_bytes > 0 ? kDirectLanes : 0);
     cudaError_t e = cudaSuccess;
+    for (Lane& ln : s->lanes) {
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ln.ev, cudaEventDisableTiming);
+    }
     for (Slot& sl : s->slots) {
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
@@ -303,6 +392,10 @@ CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_bud
     }
     if (e != cudaSuccess) {
         ckg::set_last_error(cudaGetErrorString(e));
+        for (Lane& ln : s->lanes) {
+            if (ln.ev) cudaEventDestroy(ln.ev);
+            if (ln.stream) cudaStreamDestroy(ln.stream);
+        }
         for (Slot& sl : s->slots) {
             ckg::free_run_slot(&sl.run);
             if (sl.ev) cudaEventDestroy(sl.ev);
@@ -327,6 +420,11 @@ void CkFftCudaServerDestroy(CkFftCudaServer* s)
         ckg::free_run_slot(&sl.run);
         if (sl.ev) cudaEventDestroy(sl.ev);
         if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    for (Lane& ln : s->lanes) {
+        if (ln.stream) cudaStreamSynchronize(ln.stream);
+        if (ln.ev) cudaEventDestroy(ln.ev);
+        if (ln.stream) cudaStreamDestroy(ln.stream);
     }
     delete s;
 }

@@ -201,7 +201,12 @@ typedef struct
 }
 CkFftCudaServeStats;
 
-CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_budget_bytes, int max_inflight);
+/* max_inflight: job-kernel runs on the GPU at once (1..16).
+ * direct_threshold_bytes: requests whose algorithmic bytes (each transform
+ * read once and written once) reach this size skip batching and run through
+ * the batched entry points on one of two direct lanes; 0 batches everything. */
+CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_budget_bytes, int max_inflight,
+                                       long long direct_threshold_bytes);
 void CkFftCudaServerDestroy(CkFftCudaServer* server);   /* finishes admitted work first */
 
 /* Queues one request (validated like a job; device buffers).  Returns a ticket

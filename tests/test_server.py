@@ -47,7 +47,7 @@ def test_results_same_alone_and_in_the_mix(torch_cuda, ctx_cache, oracle_mod):
     from ckfft_gb300 import binding
     torch = torch_cuda
     ctx = ctx_cache(1 << 20)
-    srv = binding.Server(ctx, scratch_budget_bytes=256 << 20, max_inflight=3)
+    srv = binding.Server(ctx, scratch_budget_bytes=256 << 20, max_inflight=3, direct_threshold_bytes=0)
     reqs = reqs_mix(torch, 7)
     tickets = [srv.submit(*r) for r in reqs]              # all at once: many share runs
     assert all(t > 0 for t in tickets)
@@ -74,7 +74,7 @@ def test_replay_trace_and_per_request_path(torch_cuda, ctx_cache):
     from ckfft_gb300 import binding
     torch = torch_cuda
     ctx = ctx_cache(1 << 20)
-    srv = binding.Server(ctx, scratch_budget_bytes=512 << 20, max_inflight=3)
+    srv = binding.Server(ctx, scratch_budget_bytes=512 << 20, max_inflight=3, direct_threshold_bytes=4 << 20)
     reqs = reqs_mix(torch, 8)
     rng = np.random.default_rng(9)
     t = np.cumsum(rng.exponential(20e-6, len(reqs)))
@@ -102,7 +102,7 @@ def test_request_larger_than_the_scratch_arena(torch_cuda, ctx_cache, oracle_mod
     from ckfft_gb300 import binding
     torch = torch_cuda
     ctx = ctx_cache(1 << 18)
-    srv = binding.Server(ctx, scratch_budget_bytes=2 << 20, max_inflight=2)
+    srv = binding.Server(ctx, scratch_budget_bytes=2 << 20, max_inflight=2, direct_threshold_bytes=0)
     rng = np.random.default_rng(3)
     r = make_req(torch, rng, "cfwd", 1 << 18, 1)
     ok, _ = srv.wait(srv.submit(*r), 30.0)
