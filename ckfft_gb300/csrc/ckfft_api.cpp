@@ -523,7 +523,10 @@ int CkFftRealInverse(CkFftContext* c, int n, const CkFftComplex* in, float* out,
     if (needs_large(w)) {
         DeviceScope scope(c->device);
         Mem where;
-        if (scope.ok && classify(tmpBuf, c->device, &where) && where == Mem::Device) {
+        // (256-byte alignment: the row pass drops the dead intermediate's
+        // 128-byte L2 lines after reading them)
+        if (scope.ok && ((uintptr_t)tmpBuf & 255) == 0 && classify(tmpBuf, c->device, &where) &&
+            where == Mem::Device) {
             scratch = tmpBuf;
             scratch_bytes = sizeof(CkFftComplex) * (size_t)(n / 2 + 1);
         }

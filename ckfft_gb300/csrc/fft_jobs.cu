@@ -103,17 +103,17 @@ __device__ __forceinline__ float2* pick(const LargeDesc& d, int sel)
 template <int OP, int LS>
 __device__ __noinline__ void run_pass(const Unit& u, const JobsArgs& a, float2* smem)
 {
-    using P = PassCfg<LS>;
+    using P = PassCfg<LS, kJobThreads>;
     const int s = threadIdx.x / P::THREADS, tid = threadIdx.x % P::THREADS;
     const LargeDesc d = a.large[u.job];
     const float2* src = pick(d, u.sel & 15);
     float2* dst = pick(d, u.sel >> 4);
     float2* my = smem + s * P::SLOTS;
     const long long tile = (long long)u.first + s;
-    if constexpr (OP == U_COLS_FWD) pass_cols<LS, false, true>(src, dst, u.log2b, tile, tid, my, a.tw);
-    else if constexpr (OP == U_COLS_INV) pass_cols<LS, true, true>(src, dst, u.log2b, tile, tid, my, a.tw);
-    else if constexpr (OP == U_ROWS_FWD) pass_rows<LS, false, true>(src, dst, u.log2b, tile, tid, my, a.tw);
-    else pass_rows<LS, true, true>(src, dst, u.log2b, tile, tid, my, a.tw);
+    if constexpr (OP == U_COLS_FWD) pass_cols<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_COLS_INV) pass_cols<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_ROWS_FWD) pass_rows<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else pass_rows<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
 }
 
 __device__ __noinline__ void run_split_merge(const Unit& u, const JobsArgs& a)
@@ -146,12 +146,12 @@ __device__ __noinline__ void run_split_merge(const Unit& u, const JobsArgs& a)
     case 10: run_single<OP, 10>(u, a, smem); break;                                   \
     case 11: run_single<OP, 11>(u, a, smem); break;                                   \
     case 12: run_single<OP, 12>(u, a, smem); break;                                   \
-    case 13: run_single<OP, 13>(u, a, smem); break;                                   \
     default: break;                                                                   \
     }
 
 #define CKG_PASS_CASES(OP)                                                            \
     switch (u.log2a) {                                                                \
+    case 6: run_pass<OP, 6>(u, a, smem); break;                                       \
     case 7: run_pass<OP, 7>(u, a, smem); break;                                       \
     case 8: run_pass<OP, 8>(u, a, smem); break;                                       \
     case 9: run_pass<OP, 9>(u, a, smem); break;                                       \
@@ -190,7 +190,7 @@ __device__ __forceinline__ void dispatch(const Unit& u, const JobsArgs& a, float
     }
 }
 
-__global__ void __launch_bounds__(kJobThreads, 2) k_jobs(JobsArgs a)
+__global__ void __launch_bounds__(kJobThreads, kJobCtasPerSm) k_jobs(JobsArgs a)
 {
     extern __shared__ __align__(128) float2 smem[];
     __shared__ int s_unit;
@@ -232,19 +232,20 @@ constexpr size_t single_smem()
 template <int LS>
 constexpr size_t pass_smem()
 {
-    return PassCfg<LS>::SMEM * (kJobThreads / PassCfg<LS>::THREADS);
+    return PassCfg<LS, kJobThreads>::SMEM * (kJobThreads / PassCfg<LS, kJobThreads>::THREADS);
 }
 constexpr size_t cmax(size_t a, size_t b) { return a > b ? a : b; }
 
 size_t jobs_smem_bytes()
 {
     size_t m = 0;
+    m = cmax(m, single_smem<0>()); m = cmax(m, single_smem<1>());
     m = cmax(m, single_smem<2>()); m = cmax(m, single_smem<3>()); m = cmax(m, single_smem<4>());
     m = cmax(m, single_smem<5>()); m = cmax(m, single_smem<6>()); m = cmax(m, single_smem<7>());
     m = cmax(m, single_smem<8>()); m = cmax(m, single_smem<9>()); m = cmax(m, single_smem<10>());
-    m = cmax(m, single_smem<11>()); m = cmax(m, single_smem<12>()); m = cmax(m, single_smem<13>());
-    m = cmax(m, pass_smem<7>()); m = cmax(m, pass_smem<8>()); m = cmax(m, pass_smem<9>());
-    m = cmax(m, pass_smem<10>());
+    m = cmax(m, single_smem<11>()); m = cmax(m, single_smem<12>());
+    m = cmax(m, pass_smem<6>()); m = cmax(m, pass_smem<7>()); m = cmax(m, pass_smem<8>());
+    m = cmax(m, pass_smem<9>()); m = cmax(m, pass_smem<10>());
     return (m + 127) / 128 * 128;
 }
 

@@ -111,7 +111,9 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
 }
 
 // Row pass for tile `tile` (rows tile*C .. tile*C+C-1) of one transform.
-template <int LB, bool INV, bool CG, int MAXT = 512>
+// DISCARD: the input is a dead intermediate (scratch) whose L2 lines may be
+// dropped without write-back once read; it must be 128-byte aligned.
+template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true>
 __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
                                           long long tile, int tid, float2* smem, const float2* __restrict__ tw)
 {
@@ -127,6 +129,15 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
     PaddedView view{smem + r * padded_len(N2)};
     stockham<LB, P::LOG2R, INV, (P::T <= 32)>(v, t, tw, view);
     __syncthreads();
+    if constexpr (DISCARD) {
+        // every thread of the tile has consumed its inputs: the intermediate
+        // rows are dead, so drop their L2 lines instead of writing them back
+        static_assert(N2 % 16 == 0, "rows span whole 128-byte lines");
+        const char* row = (const char*)(in + (row0 + r) * N2);
+#pragma unroll
+        for (int l = t; l < N2 / 16; l += P::T)
+            asm volatile("discard.global.L2 [%0], 128;" ::"l"(row + 128 * l) : "memory");
+    }
     // transpose through shared memory so that stores run along rows k1
 #pragma unroll
     for (int m = 0; m < P::R; ++m) smem[TileView<P::C>::slot(t + m * P::T, r)] = v[m];

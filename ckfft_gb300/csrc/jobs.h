@@ -70,12 +70,17 @@ struct JobsArgs {
     unsigned* err;
 };
 
-constexpr int kJobThreads = 512;
+// 256 threads per CTA and 64 registers: four CTAs -- four independent unit
+// streams -- per SM, which hides the latency of each unit's start (queue
+// claim, descriptor, frame pointers) better than two larger CTAs.
+constexpr int kJobThreads = 256;
+constexpr int kJobCtasPerSm = 4;
 
 // Largest multi-pass size the job kernel handles (sub-lengths up to 2^10).
 constexpr int kJobMaxLog2Complex = 20;
-// Single-CTA sizes inside the job kernel (complex length, 64 registers).
-constexpr int kJobMaxSingleLog2 = 13;
+// Single-CTA sizes inside the job kernel (complex length); 2^13 and up run
+// as column / row passes.
+constexpr int kJobMaxSingleLog2 = 12;
 
 struct ContextView;
 

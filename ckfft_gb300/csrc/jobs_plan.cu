@@ -29,10 +29,11 @@ struct PassShape {
 static PassShape pass_shape(int ls)
 {
     switch (ls) {
-    case 7: return {PassCfg<7>::THREADS, PassCfg<7>::C};
-    case 8: return {PassCfg<8>::THREADS, PassCfg<8>::C};
-    case 9: return {PassCfg<9>::THREADS, PassCfg<9>::C};
-    case 10: return {PassCfg<10>::THREADS, PassCfg<10>::C};
+    case 6: return {PassCfg<6, kJobThreads>::THREADS, PassCfg<6, kJobThreads>::C};
+    case 7: return {PassCfg<7, kJobThreads>::THREADS, PassCfg<7, kJobThreads>::C};
+    case 8: return {PassCfg<8, kJobThreads>::THREADS, PassCfg<8, kJobThreads>::C};
+    case 9: return {PassCfg<9, kJobThreads>::THREADS, PassCfg<9, kJobThreads>::C};
+    case 10: return {PassCfg<10, kJobThreads>::THREADS, PassCfg<10, kJobThreads>::C};
     default: return {0, 0};
     }
 }
@@ -59,7 +60,7 @@ static int single_threads(int l)
     }
 }
 
-constexpr int kElemsPerUnit = kJobThreads * 8;   // split / merge work per unit
+constexpr int kElemsPerUnit = kJobThreads * 16;  // split / merge work per unit
 
 struct Built {
     std::vector<Unit> units;
