@@ -262,6 +262,9 @@ cudaError_t enqueue(const CkFftContext* c, const Work& w, long long cnt, const v
     if (cnt <= 0) return cudaSuccess;
     if (is_real(w.kind) && w.n <= 4)
         return ckg::launch_real_tiny(w.kind, w.n, din, dout, cnt, w.in_dist, w.out_dist, s);
+    if (!is_real(w.kind) && ckg::cluster_supported(w.log2n) && ckg::cluster_enabled())
+        return ckg::launch_cluster_c2c(w.kind == ckg::C2C_INV, w.log2n, din, dout, cnt, w.in_dist, w.out_dist,
+                                       c->dtw, s);
     if (!needs_large(w))
         return ckg::launch_small(w.kind, w.log2n, din, dout, cnt, w.in_dist, w.out_dist, c->dtw, s);
     switch (w.kind) {
@@ -284,6 +287,7 @@ cudaError_t enqueue(const CkFftContext* c, const Work& w, long long cnt, const v
 size_t scratch_need(const Work& w, long long cnt)
 {
     if (!needs_large(w)) return 0;
+    if (!is_real(w.kind) && ckg::cluster_supported(w.log2n) && ckg::cluster_enabled()) return 0;
     const size_t one = ckg::large_scratch_bytes(w.kind, w.log2n);
     const size_t cap = 256ull << 20;
     long long g = (long long)(cap / one);

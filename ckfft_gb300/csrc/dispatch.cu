@@ -15,6 +15,20 @@ cudaError_t prepare_small_c2c();
 cudaError_t prepare_small_real();
 cudaError_t prepare_large();
 cudaError_t prepare_jobs();
+cudaError_t prepare_cluster();
+
+// Opt-in (CKFFT_CUDA_CLUSTER=1): measured slower than the default paths on
+// GB300 (2^14: 2366 vs 3669 GB/s single CTA; 2^15 / 2^16: 1936 / 1516 vs about
+// 2810 GB/s in two passes), because the cluster exchanges cost more than the
+// HBM pass they save.
+bool cluster_enabled()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("CKFFT_CUDA_CLUSTER");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
 
 static std::atomic<long long> g_launches{0};
 
@@ -137,6 +151,7 @@ cudaError_t prepare_device()
     if ((e = prepare_small_real()) != cudaSuccess) return e;
     if ((e = prepare_large()) != cudaSuccess) return e;
     if ((e = prepare_jobs()) != cudaSuccess) return e;
+    if ((e = prepare_cluster()) != cudaSuccess) return e;
     if (dev < 64) done |= 1ull << dev;
     return cudaSuccess;
 }

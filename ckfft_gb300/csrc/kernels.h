@@ -51,6 +51,13 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
 cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long count,
                              long long in_dist, long long out_dist, const float2* tw,
                              void* scratch, size_t scratch_bytes, cudaStream_t stream);
+// Single-pass complex transforms of 2^14 .. 2^16 on thread-block clusters
+// (fft_cluster.cu).  cluster_enabled(): only with CKFFT_CUDA_CLUSTER=1.
+bool cluster_supported(int log2n);
+bool cluster_enabled();
+cudaError_t launch_cluster_c2c(bool inverse, int log2n, const void* in, void* out, long long count,
+                               long long in_dist, long long out_dist, const float2* tw, cudaStream_t stream);
+
 // Scratch bytes one transform of the given kind and size needs on the large path.
 size_t large_scratch_bytes(Kind kind, int log2n);
 
