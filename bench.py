@@ -361,7 +361,9 @@ def measure_e2e(torch, ctx, x, n, frames, bytes_step, world, steps=3):
     d2h = Xh.numel() * 8 + yh.numel() * 4
     return {"value": round(world * bytes_step / dt / 1e9, 2), "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": round(dt * 1e3, 3),
-            "steps": steps, "api": "CkFftCudaRealForwardBatch + CkFftCudaRealInverseBatch on pinned host buffers"}
+            "steps": steps, "api": "CkFftCudaRealForwardBatch + CkFftCudaRealInverseBatch on pinned host buffers",
+            "route": "real inverse read and written in place by the kernel over the CPU-GPU link; "
+                     "real forward (ragged n/2+1 rows, > 128 MiB) staged by copy engines"}
 
 
 def measure_per_call(torch, ctx, x, n, calls=512):

@@ -8,12 +8,16 @@
 // twiddle tables in device memory, and every transform runs as CUDA kernels.
 //
 // Pointer handling: device and managed pointers on the context's device are
-// used in place; host pointers (pageable or pinned) are moved through
-// device-resident staging buffers, split into chunks that run on three
-// streams so that host->device copies, kernels and device->host copies of
-// consecutive chunks overlap.
+// used in place.  Page-locked host buffers of single-CTA sizes are read and
+// written by the kernels themselves over the CPU-GPU link (one crossing per
+// byte, no staging copy; CKFFT_CUDA_ZERO_COPY=0 turns this off).  Other host
+// pointers (pageable, or multi-pass sizes) are moved through device-resident
+// staging buffers, split into chunks that run on three streams so that
+// host->device copies, kernels and device->host copies of consecutive chunks
+// overlap.
 #include "ckfft_cuda.h"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -204,6 +208,57 @@ bool classify(const void* p, int dev, Mem* where)
     return true;
 }
 
+bool zero_copy_enabled()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("CKFFT_CUDA_ZERO_COPY");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+// cuPointerGetAttribute, taken from the driver through the runtime (the
+// library links the runtime only).
+using PtrAttrFn = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+
+PtrAttrFn ptr_attr_fn()
+{
+    static const PtrAttrFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (PtrAttrFn) nullptr;
+        }
+        return (PtrAttrFn)f;
+    }();
+    return fn;
+}
+
+// True when [p, p + bytes) lies inside ONE page-locked host allocation that
+// the current device addresses at the same pointer, so that kernels may read
+// or write the whole range in place.  Anything else (pageable memory, a range
+// that runs past its allocation) answers false and is staged.
+bool mapped_host(const void* p, size_t bytes)
+{
+    if (!zero_copy_enabled() || bytes == 0) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer != p) return false;
+    const PtrAttrFn fn = ptr_attr_fn();
+    if (!fn) return false;
+    unsigned long long first = 0, last = 0;
+    if (fn(&first, CU_POINTER_ATTRIBUTE_BUFFER_ID, (CUdeviceptr)(uintptr_t)p) != CUDA_SUCCESS) return false;
+    if (fn(&last, CU_POINTER_ATTRIBUTE_BUFFER_ID, (CUdeviceptr)((uintptr_t)p + bytes - 1)) != CUDA_SUCCESS)
+        return false;
+    return first != 0 && first == last;
+}
+
 // One transform family request.
 struct Work {
     ckg::Kind kind;
@@ -296,8 +351,57 @@ size_t scratch_need(const Work& w, long long cnt)
     return one * (size_t)g;
 }
 
+// Whether kernels reading and writing page-locked host memory in place beat
+// the staged copy pipeline.  Measured on GB300 (real n = 4096, page-locked
+// input and output): in place wins at every batch size when each output row
+// is whole 128-byte lines (real inverse: 307 vs 247 GB/s at 65536 frames) and
+// for every small call (one frame: 13.6 vs 21.4 us); with ragged output rows
+// (real forward, n/2+1 complex) the kernels' partial-line writes to host
+// memory cost more than the staged copies beyond about 128 MiB of output
+// (258 vs 277 GB/s at 16384 frames, 266 vs 316 at 65536).
+bool zero_copy_pays(const Work& w, bool host_out)
+{
+    if (!host_out || w.out_bytes % 128 == 0) return true;
+    return (size_t)w.count * w.out_bytes <= (128ull << 20);
+}
+
+// Blocking run whose host-side buffers are mapped page-locked memory: one
+// launch over the whole batch on a lane stream, kernels reading and writing
+// the host memory in place (plain loads for a host input).
+int run_direct(CkFftContext* c, const Work& w, const void* in, void* out, bool host_in, cudaStream_t user_stream)
+{
+    Lane* lane = acquire_lane(c);
+    if (!lane) return fail("cannot create a staging lane (CUDA streams)");
+    Slot& sl = lane->slot[0];
+    cudaError_t e = cudaSuccess;
+    const char* where = "kernel launch";
+    cudaEvent_t dep = nullptr;
+    if (user_stream) {
+        if ((e = cudaEventCreateWithFlags(&dep, cudaEventDisableTiming)) != cudaSuccess) where = "cudaEventCreate";
+        else if ((e = cudaEventRecord(dep, user_stream)) != cudaSuccess) where = "cudaEventRecord";
+        else if ((e = cudaStreamWaitEvent(sl.stream, dep, 0)) != cudaSuccess) where = "cudaStreamWaitEvent";
+    }
+    if (e == cudaSuccess) {
+        if (host_in) {
+            ckg::PlainLoadsScope plain;
+            e = enqueue(c, w, w.count, in, out, nullptr, 0, sl.stream);
+        } else {
+            e = enqueue(c, w, w.count, in, out, nullptr, 0, sl.stream);
+        }
+    }
+    const cudaError_t se = cudaStreamSynchronize(sl.stream);
+    if (e == cudaSuccess && se != cudaSuccess) { e = se; where = "cudaStreamSynchronize"; }
+    if (dep) cudaEventDestroy(dep);
+    release_lane(c, lane);
+    if (e != cudaSuccess) return cuda_fail(where, e);
+    if (ckg::take_device_error()) return fail("a kernel's bounded wait for its input copy timed out");
+    return 1;
+}
+
 // Runs a request.  stream != NULL with device pointers: asynchronous on that
-// stream.  Otherwise blocking, through a lane of the context's pool.
+// stream.  Mapped page-locked host buffers of single-CTA sizes: one blocking
+// launch in place.  Otherwise blocking, staged through a lane of the
+// context's pool.
 int run(CkFftContext* c, const Work& w, const void* in, void* out, cudaStream_t user_stream,
         void* user_scratch = nullptr, size_t user_scratch_bytes = 0)
 {
@@ -320,6 +424,10 @@ int run(CkFftContext* c, const Work& w, const void* in, void* out, cudaStream_t 
         if (e != cudaSuccess) return cuda_fail("kernel launch", e);
         return 1;
     }
+    if (!needs_large(w) && (min == Mem::Host || mout == Mem::Host) && zero_copy_pays(w, mout == Mem::Host) &&
+        (min == Mem::Device || mapped_host(in, (size_t)w.count * w.in_bytes)) &&
+        (mout == Mem::Device || mapped_host(out, (size_t)w.count * w.out_bytes)))
+        return run_direct(c, w, in, out, min == Mem::Host, user_stream);
 
     Lane* lane = acquire_lane(c);
     if (!lane) return fail("cannot create a staging lane (CUDA streams)");

@@ -50,8 +50,14 @@ cudaError_t launch_small(Kind kind, int log2n, const void* in, void* out, long l
     return e;
 }
 
+static thread_local int t_plain_loads = 0;
+
+PlainLoadsScope::PlainLoadsScope() : prev(t_plain_loads) { t_plain_loads = 1; }
+PlainLoadsScope::~PlainLoadsScope() { t_plain_loads = prev; }
+
 int variant_for(Kind kind, int log2c)
 {
+    if (t_plain_loads) return 0;
     static const int forced = [] {
         const char* v = std::getenv("CKFFT_CUDA_PIPE_NBUF");
         if (!v || !*v) return -1;

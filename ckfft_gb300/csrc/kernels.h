@@ -88,6 +88,14 @@ constexpr int kPipeMinLog2 = 6;
 // unless the CKFFT_CUDA_PIPE_NBUF environment variable forces one variant
 // (the autotuner uses it to measure each variant).
 int variant_for(Kind kind, int log2c);
+// While one of these lives on a thread, variant_for() answers 0 on that
+// thread: launches whose input is host memory mapped into the device's
+// address space read it with plain loads, never with bulk (TMA) copies.
+struct PlainLoadsScope {
+    PlainLoadsScope();
+    ~PlainLoadsScope();
+    int prev;
+};
 // Device word (in mapped host memory) where kernels record a timed-out wait,
 // for the current device; take_device_error() reads and clears it.
 unsigned* device_error_word();

@@ -5,6 +5,10 @@ Bar (conftest.assert_close): relative L2 <= 1e-5 and max element error
 <= 2e-6 * log2 n of the reference's rms; closed-form sizes are bit-exact.
 """
 import ctypes as C
+import os
+import pathlib
+import subprocess
+import sys
 import threading
 
 import numpy as np
@@ -268,6 +272,64 @@ def test_staged_batch_spans_chunks(torch_cuda, ctx_cache):
     ref = run_batch(torch_cuda, ctx, "cfwd", n, x, where="device")
     assert bits_equal(run_batch(torch_cuda, ctx, "cfwd", n, x, where="pinned"), ref)
     assert bits_equal(run_batch(torch_cuda, ctx, "cfwd", n, x, where="host"), ref)
+
+
+@pytest.mark.parametrize("kind", ["cfwd", "rfwd", "rinv"])
+def test_pinned_batch_runs_in_place(torch_cuda, ctx_cache, lib, kind):
+    """Page-locked host buffers of a single-CTA size are read and written by
+    one launch in place (no staging chunks), alone or mixed with device
+    buffers, with the bits of the all-device run."""
+    torch = torch_cuda
+    n, frames = 4096, 2600                 # more than one 64 MiB staging chunk
+    ctx = ctx_cache(n)
+    rng = np.random.default_rng(19)
+    if kind == "rfwd":
+        x = rng.uniform(-1, 1, (frames, n)).astype(np.float32)
+    else:
+        m = n // 2 + 1 if kind == "rinv" else n
+        x = (rng.uniform(-1, 1, (frames, m)) + 1j * rng.uniform(-1, 1, (frames, m))).astype(np.complex64)
+    ref = run_batch(torch, ctx, kind, n, x, where="device")
+    m, dt = OUT_SHAPE[kind](n)
+    tdt = torch.complex64 if dt == np.complex64 else torch.float32
+    xh = torch.from_numpy(x).pin_memory()
+    xd = xh.cuda()
+    for src in (xh, xd):
+        for dst_dev in (False, True):
+            if src is xd and dst_dev:
+                continue
+            out = torch.zeros((frames, m), dtype=tdt, device="cuda" if dst_dev else "cpu")
+            if not dst_dev:
+                out = out.pin_memory()
+            before = lib.CkFftCudaLaunchCount()
+            ctx.check(ctx.batch(kind, n, frames, src, out))
+            assert lib.CkFftCudaLaunchCount() - before == 1
+            assert bits_equal(out.cpu().numpy(), ref)
+
+
+def test_zero_copy_switch_stages_pinned(torch_cuda):
+    """CKFFT_CUDA_ZERO_COPY=0 moves pinned buffers through the staging chunks
+    (several launches) and gives the same bits."""
+    code = r"""
+import numpy as np, torch
+from ckfft_gb300 import binding
+lib = binding.load()
+ctx = binding.Context(4096)
+rng = np.random.default_rng(19)
+x = (rng.uniform(-1, 1, (2600, 4096)) + 1j * rng.uniform(-1, 1, (2600, 4096))).astype(np.complex64)
+xh = torch.from_numpy(x).pin_memory()
+yh = torch.zeros_like(xh).pin_memory()
+yd = torch.zeros((2600, 4096), dtype=torch.complex64, device="cuda")
+ctx.check(ctx.batch("cfwd", 4096, 2600, xh.cuda(), yd))
+before = lib.CkFftCudaLaunchCount()
+ctx.check(ctx.batch("cfwd", 4096, 2600, xh, yh))
+assert lib.CkFftCudaLaunchCount() - before >= 2
+assert np.array_equal(yh.numpy().view(np.uint32), yd.cpu().numpy().view(np.uint32))
+print("ok")
+"""
+    env = dict(os.environ, CKFFT_CUDA_ZERO_COPY="0")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600,
+                       cwd=str(pathlib.Path(__file__).resolve().parents[1]))
+    assert r.returncode == 0 and "ok" in r.stdout, r.stdout + r.stderr
 
 
 def test_zero_count_is_noop(torch_cuda, ctx_cache):
