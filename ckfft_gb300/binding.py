@@ -77,6 +77,11 @@ def _declare_extras(lib):
     if hasattr(lib, "CkFftCudaComplexBatchNoAlloc"):
         lib.CkFftCudaComplexBatchNoAlloc.restype = i
         lib.CkFftCudaComplexBatchNoAlloc.argtypes = [vp, i, i, i, vp, vp, vp]
+    for f in ("CkFftCudaComplexForwardStrided", "CkFftCudaComplexInverseStrided",
+              "CkFftCudaRealForwardStrided", "CkFftCudaRealInverseStrided"):
+        if hasattr(lib, f):
+            getattr(lib, f).restype = i
+            getattr(lib, f).argtypes = [vp, i, ll, vp, ll, ll, vp, ll, ll, vp]
     if hasattr(lib, "CkFftCudaServerCreate"):
         lib.CkFftCudaServerCreate.restype = vp
         lib.CkFftCudaServerCreate.argtypes = [vp, C.c_size_t, i, ll]
@@ -206,6 +211,19 @@ class Context:
         }[kind]
         s = getattr(stream, "cuda_stream", stream)
         return fn(self.handle, n, count, ptr(inp), ptr(out), s)
+
+    def strided(self, kind: str, n: int, count: int, inp, in_stride: int, in_dist: int,
+                out, out_stride: int, out_dist: int, stream=None) -> int:
+        """Advanced-layout batch: element p of transform f at inp[f*in_dist + p*in_stride]
+        -> out[f*out_dist + p*out_stride] (elements of each side's type)."""
+        fn = {
+            "cfwd": self.lib.CkFftCudaComplexForwardStrided,
+            "cinv": self.lib.CkFftCudaComplexInverseStrided,
+            "rfwd": self.lib.CkFftCudaRealForwardStrided,
+            "rinv": self.lib.CkFftCudaRealInverseStrided,
+        }[kind]
+        s = getattr(stream, "cuda_stream", stream)
+        return fn(self.handle, n, count, ptr(inp), in_stride, in_dist, ptr(out), out_stride, out_dist, s)
 
     def run_jobs(self, jobs, stream=None) -> int:
         arr, n = job_array(jobs)

@@ -241,9 +241,9 @@ PtrAttrFn ptr_attr_fn()
 // the current device addresses at the same pointer, so that kernels may read
 // or write the whole range in place.  Anything else (pageable memory, a range
 // that runs past its allocation) answers false and is staged.
-bool mapped_host(const void* p, size_t bytes)
+bool mapped_range(const void* p, size_t bytes)
 {
-    if (!zero_copy_enabled() || bytes == 0) return false;
+    if (bytes == 0) return false;
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
@@ -258,6 +258,8 @@ bool mapped_host(const void* p, size_t bytes)
         return false;
     return first != 0 && first == last;
 }
+
+bool mapped_host(const void* p, size_t bytes) { return zero_copy_enabled() && mapped_range(p, bytes); }
 
 // One transform family request.
 struct Work {
@@ -517,6 +519,137 @@ int check_call(const CkFftContext* c, bool inverse, int n, const void* in, const
     return 1;
 }
 
+// ------------------------------------------------------------ strided batches
+
+// Enqueues an advanced-layout batch on `s` (buffers the device can address).
+cudaError_t enqueue_strided(CkFftContext* c, const Work& w, const void* in, long long is, void* out, long long os,
+                            cudaStream_t s)
+{
+    const bool rin = w.kind == ckg::R2C, rout = w.kind == ckg::C2R;
+    // contiguous rows at any distance: the batched kernels read them directly
+    // (real rows as packed pairs: 8-byte aligned, even distance)
+    const bool rows = is == 1 && os == 1 &&
+                      (!rin || (w.in_dist % 2 == 0 && ((uintptr_t)in & 7) == 0)) &&
+                      (!rout || (w.out_dist % 2 == 0 && ((uintptr_t)out & 7) == 0));
+    cudaError_t e;
+    if (rows) {
+        const size_t need = scratch_need(w, w.count);
+        void* scratch = nullptr;
+        if (need && (e = ckg::pool_alloc_async(&scratch, need, s)) != cudaSuccess) return e;
+        e = enqueue(c, w, w.count, in, out, scratch, need, s);
+        if (scratch) cudaFreeAsync(scratch, s);
+        return e;
+    }
+    if (ckg::strided_supported(w.kind, w.log2n))
+        return ckg::launch_strided(w.kind, w.log2n, in, out, w.count, ckg::Layout{is, w.in_dist, os, w.out_dist},
+                                   c->dtw, s);
+    // gather -> contiguous transform -> scatter, in groups of bounded scratch
+    const int ein = rin ? 4 : 8, eout = rout ? 4 : 8;
+    const long long ni = (long long)(w.in_bytes / ein), no = (long long)(w.out_bytes / eout);
+    const size_t per = w.in_bytes + w.out_bytes;
+    long long g = (long long)((256ull << 20) / per);
+    if (g < 1) g = 1;
+    if (g > w.count) g = w.count;
+    const size_t rows_in = (w.in_bytes * (size_t)g + 255) & ~(size_t)255;
+    const size_t rows_out = (w.out_bytes * (size_t)g + 255) & ~(size_t)255;
+    const size_t large = scratch_need(w, g);
+    void* block = nullptr;
+    if ((e = ckg::pool_alloc_async(&block, rows_in + rows_out + large, s)) != cudaSuccess) return e;
+    char* tin = (char*)block;
+    char* tout = tin + rows_in;
+    void* tl = large ? (void*)(tout + rows_out) : nullptr;
+    for (long long off = 0; off < w.count && e == cudaSuccess; off += g) {
+        const long long cnt = w.count - off < g ? w.count - off : g;
+        const Work wc = make_work(w.kind, w.n, cnt);
+        e = ckg::launch_gather((const char*)in + (size_t)(off * w.in_dist) * ein, is, w.in_dist, tin, cnt, ni, ein, s);
+        if (e == cudaSuccess) e = enqueue(c, wc, cnt, tin, tout, tl, large, s);
+        if (e == cudaSuccess)
+            e = ckg::launch_scatter(tout, (char*)out + (size_t)(off * w.out_dist) * eout, os, w.out_dist, cnt, no,
+                                    eout, s);
+    }
+    cudaFreeAsync(block, s);
+    return e;
+}
+
+// Validation of an advanced layout (after check_call): element counts,
+// non-overlapping output transforms, disjoint input and output ranges.
+// On success sets the byte spans of both sides.
+int check_layout(const Work& w, const void* in, long long is, long long id, const void* out, long long os,
+                 long long od, size_t* in_span, size_t* out_span)
+{
+    if (is < 1 || os < 1) return fail("strides must be >= 1");
+    if (id < 0 || od < 0) return fail("distances must be >= 0");
+    const int ein = w.kind == ckg::R2C ? 4 : 8, eout = w.kind == ckg::C2R ? 4 : 8;
+    const __int128 ni = (__int128)(w.in_bytes / ein), no = (__int128)(w.out_bytes / eout);
+    const __int128 cnt = w.count;
+    if (cnt > 1) {
+        const bool side = (__int128)od >= (no - 1) * os + 1;
+        const bool inter = od >= 1 && (__int128)os >= (cnt - 1) * od + 1;
+        if (!side && !inter) return fail("output transforms overlap (stride / distance)");
+    }
+    const __int128 si = ((cnt - 1) * id + (ni - 1) * is + 1) * ein;
+    const __int128 so = ((cnt - 1) * od + (no - 1) * os + 1) * eout;
+    const __int128 lim = (__int128)1 << 62;
+    if (si > lim || so > lim) return fail("layout spans more than 2^62 bytes");
+    const uintptr_t a0 = (uintptr_t)in, a1 = a0 + (uintptr_t)si, b0 = (uintptr_t)out, b1 = b0 + (uintptr_t)so;
+    if (a1 < a0 || b1 < b0) return fail("layout wraps the address space");
+    if (a0 < b1 && b0 < a1) return fail("input and output ranges overlap");
+    *in_span = (size_t)si;
+    *out_span = (size_t)so;
+    return 1;
+}
+
+int strided_call(CkFftContext* c, ckg::Kind kind, int n, long long count, const void* in, long long is,
+                 long long id, void* out, long long os, long long od, void* stream)
+{
+    const bool inverse = kind == ckg::C2C_INV || kind == ckg::C2R;
+    if (!check_call(c, inverse, n, in, out, count)) return 0;
+    if (count > 0x7fffffffLL) return fail("count must be below 2^31");
+    Work w = make_work(kind, n, count);
+    if (count == 0) return 1;
+    size_t in_span = 0, out_span = 0;
+    if (!check_layout(w, in, is, id, out, os, od, &in_span, &out_span)) return 0;
+    w.in_dist = id;
+    w.out_dist = od;
+    DeviceScope scope(c->device);
+    if (!scope.ok) return fail("cannot select the context's CUDA device");
+    Mem min, mout;
+    if (!classify(in, c->device, &min) || !classify(out, c->device, &mout)) return 0;
+    if ((min == Mem::Host && !mapped_range(in, in_span)) || (mout == Mem::Host && !mapped_range(out, out_span)))
+        return fail("strided batches need device, managed or page-locked host buffers covering the layout");
+    const cudaStream_t us = (cudaStream_t)stream;
+    if (us && min == Mem::Device && mout == Mem::Device) {
+        const cudaError_t e = enqueue_strided(c, w, in, is, out, os, us);
+        return e == cudaSuccess ? 1 : cuda_fail("kernel launch", e);
+    }
+    Lane* lane = acquire_lane(c);
+    if (!lane) return fail("cannot create a staging lane (CUDA streams)");
+    Slot& sl = lane->slot[0];
+    cudaError_t e = cudaSuccess;
+    const char* where = "kernel launch";
+    cudaEvent_t dep = nullptr;
+    if (us) {
+        if ((e = cudaEventCreateWithFlags(&dep, cudaEventDisableTiming)) != cudaSuccess) where = "cudaEventCreate";
+        else if ((e = cudaEventRecord(dep, us)) != cudaSuccess) where = "cudaEventRecord";
+        else if ((e = cudaStreamWaitEvent(sl.stream, dep, 0)) != cudaSuccess) where = "cudaStreamWaitEvent";
+    }
+    if (e == cudaSuccess) {
+        if (min == Mem::Host) {
+            ckg::PlainLoadsScope plain;
+            e = enqueue_strided(c, w, in, is, out, os, sl.stream);
+        } else {
+            e = enqueue_strided(c, w, in, is, out, os, sl.stream);
+        }
+    }
+    const cudaError_t se = cudaStreamSynchronize(sl.stream);
+    if (e == cudaSuccess && se != cudaSuccess) { e = se; where = "cudaStreamSynchronize"; }
+    if (dep) cudaEventDestroy(dep);
+    release_lane(c, lane);
+    if (e != cudaSuccess) return cuda_fail(where, e);
+    if (ckg::take_device_error()) return fail("a kernel's bounded wait for its input copy timed out");
+    return 1;
+}
+
 int complex_call(CkFftContext* c, bool inverse, int n, long long count, const CkFftComplex* in,
                  CkFftComplex* out, void* stream)
 {
@@ -673,6 +806,34 @@ int CkFftCudaRealInverseBatch(CkFftContext* c, int n, int count, const CkFftComp
 {
     if (!check_call(c, true, n, in, out, count)) return 0;
     return run(c, make_work(ckg::C2R, n, count), in, out, (cudaStream_t)stream);
+}
+
+int CkFftCudaComplexForwardStrided(CkFftContext* c, int n, long long count, const CkFftComplex* in,
+                                   long long in_stride, long long in_dist, CkFftComplex* out, long long out_stride,
+                                   long long out_dist, void* stream)
+{
+    return strided_call(c, ckg::C2C_FWD, n, count, in, in_stride, in_dist, out, out_stride, out_dist, stream);
+}
+
+int CkFftCudaComplexInverseStrided(CkFftContext* c, int n, long long count, const CkFftComplex* in,
+                                   long long in_stride, long long in_dist, CkFftComplex* out, long long out_stride,
+                                   long long out_dist, void* stream)
+{
+    return strided_call(c, ckg::C2C_INV, n, count, in, in_stride, in_dist, out, out_stride, out_dist, stream);
+}
+
+int CkFftCudaRealForwardStrided(CkFftContext* c, int n, long long count, const float* in, long long in_stride,
+                                long long in_dist, CkFftComplex* out, long long out_stride, long long out_dist,
+                                void* stream)
+{
+    return strided_call(c, ckg::R2C, n, count, in, in_stride, in_dist, out, out_stride, out_dist, stream);
+}
+
+int CkFftCudaRealInverseStrided(CkFftContext* c, int n, long long count, const CkFftComplex* in,
+                                long long in_stride, long long in_dist, float* out, long long out_stride,
+                                long long out_dist, void* stream)
+{
+    return strided_call(c, ckg::C2R, n, count, in, in_stride, in_dist, out, out_stride, out_dist, stream);
 }
 
 long long CkFftCudaLaunchCount(void) { return ckg::launch_count(); }

@@ -16,6 +16,7 @@ cudaError_t prepare_small_real();
 cudaError_t prepare_large();
 cudaError_t prepare_jobs();
 cudaError_t prepare_cluster();
+cudaError_t prepare_strided();
 
 // Opt-in (CKFFT_CUDA_CLUSTER=1): measured slower than the default paths on
 // GB300 (2^14: 2366 vs 3669 GB/s single CTA; 2^15 / 2^16: 1936 / 1516 vs about
@@ -158,6 +159,7 @@ cudaError_t prepare_device()
     if ((e = prepare_large()) != cudaSuccess) return e;
     if ((e = prepare_jobs()) != cudaSuccess) return e;
     if ((e = prepare_cluster()) != cudaSuccess) return e;
+    if ((e = prepare_strided()) != cudaSuccess) return e;
     if (dev < 64) done |= 1ull << dev;
     return cudaSuccess;
 }

@@ -101,7 +101,7 @@ k_pipe(const float2* __restrict__ in, float2* __restrict__ out, long long ngroup
 #pragma unroll
             for (int m = 0; m < C::R; ++m) view.st(t + m * C::T, v[m]);
             xsync<C::WARP>();
-            split_store<C, M>(view, out + f * out_dist, t, tw + 2 * M);
+            split_store<C, M>(view, RowOut{out + f * out_dist}, t, tw + 2 * M);
         } else {
             float2* dst = out + f * out_dist + t;
 #pragma unroll

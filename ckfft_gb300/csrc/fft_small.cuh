@@ -36,6 +36,53 @@ __device__ __forceinline__ float2 split_twiddle(float2 w_t, const float2* __rest
     else return tw_load<INV>(twn, k);
 }
 
+// ------------------------------------------------------------- accessors
+// How a frame body reaches its input and output: element i of a frame (a
+// complex value, or a packed pair of reals on the real side).
+
+// Contiguous rows, streaming loads and stores (the batched layout).
+struct RowIn {
+    const float2* __restrict__ p;
+    __device__ __forceinline__ float2 ld(long long i) const { return __ldcs(p + i); }
+    __device__ __forceinline__ float2 ldg(long long i) const { return __ldg(p + i); }
+};
+struct RowOut {
+    float2* __restrict__ p;
+    __device__ __forceinline__ void st(long long i, float2 v) const { __stcs(p + i, v); }
+};
+// Complex element i at p[i * s].  Cached loads: with interleaved frames
+// (small s, distance 1) the frames of one CTA share sectors.
+struct StrideIn {
+    const float2* __restrict__ p;
+    long long s;
+    __device__ __forceinline__ float2 ld(long long i) const { return __ldg(p + i * s); }
+    __device__ __forceinline__ float2 ldg(long long i) const { return __ldg(p + i * s); }
+};
+struct StrideOut {
+    float2* __restrict__ p;
+    long long s;
+    __device__ __forceinline__ void st(long long i, float2 v) const { p[i * s] = v; }
+};
+// Reals at p[j * s], read or written as packed pairs (x[2i], x[2i+1]).
+struct PairIn {
+    const float* __restrict__ p;
+    long long s;
+    __device__ __forceinline__ float2 ld(long long i) const
+    {
+        return make_float2(__ldg(p + 2 * i * s), __ldg(p + (2 * i + 1) * s));
+    }
+    __device__ __forceinline__ float2 ldg(long long i) const { return ld(i); }
+};
+struct PairOut {
+    float* __restrict__ p;
+    long long s;
+    __device__ __forceinline__ void st(long long i, float2 v) const
+    {
+        p[2 * i * s] = v.x;
+        p[(2 * i + 1) * s] = v.y;
+    }
+};
+
 // Real forward split of a natural-order half-length spectrum Z held in the
 // view, written as the n/2+1 = M+1 output bins.  Bins k and M-k come from the
 // same pair: with S = z_k + conj z_{M-k}, D = z_k - conj z_{M-k}, P = W_n^k D,
@@ -43,8 +90,8 @@ __device__ __forceinline__ float2 split_twiddle(float2 w_t, const float2* __rest
 // (the reference's two per-bin formulas, src/ckfft/fft_real_default.cpp:30-58,
 // share S, D and the twiddle because W_n^{M-k} = -conj W_n^k).  Thread t
 // takes k = t + mT for m < R/2; thread 0 also takes the middle bin k = M/2.
-template <class C, int M, class View>
-__device__ __forceinline__ void split_store(const View& view, float2* __restrict__ dst, int t,
+template <class C, int M, class View, class Dst>
+__device__ __forceinline__ void split_store(const View& view, const Dst& dst, int t,
                                             const float2* __restrict__ twn)
 {
     const float2 w0 = __ldg(twn + t);
@@ -56,12 +103,12 @@ __device__ __forceinline__ void split_store(const View& view, float2* __restrict
         const float sx = z0.x + z1.x, sy = z0.y - z1.y;
         const float dx = z0.x - z1.x, dy = z0.y + z1.y;
         const float px = fmaf(w.x, dx, -w.y * dy), py = fmaf(w.x, dy, w.y * dx);
-        __stcs(dst + k, make_float2(sx + py, sy - px));
-        __stcs(dst + (M - k), make_float2(sx - py, -(sy + px)));
+        dst.st(k, make_float2(sx + py, sy - px));
+        dst.st(M - k, make_float2(sx - py, -(sy + px)));
     });
     if (t == 0) {
         const float2 z = view.ld(M / 2);                // X[M/2] = 2 conj Z[M/2]
-        __stcs(dst + M / 2, make_float2(z.x + z.x, -(z.y + z.y)));
+        dst.st(M / 2, make_float2(z.x + z.x, -(z.y + z.y)));
     }
 }
 
@@ -71,15 +118,15 @@ __device__ __forceinline__ void split_store(const View& view, float2* __restrict
 // touching memory.  Used by the batched kernels below and by the persistent
 // job kernel (fft_jobs.cu).
 
-template <int L, bool INV>
-__device__ __forceinline__ void frame_c2c(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
-                                          int t, const PaddedView& view, const float2* __restrict__ tw)
+template <int L, bool INV, class Src, class Dst>
+__device__ __forceinline__ void frame_c2c_at(const Src& src, const Dst& dst, bool live, int t,
+                                             const PaddedView& view, const float2* __restrict__ tw)
 {
     using C = SmallCfg<L>;
     float2 v[C::R];
     if (live) {
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) v[m] = __ldcs(src + t + m * C::T);
+        for (int m = 0; m < C::R; ++m) v[m] = src.ld(t + m * C::T);
     } else {
 #pragma unroll
         for (int m = 0; m < C::R; ++m) v[m] = make_float2(0.f, 0.f);
@@ -87,21 +134,28 @@ __device__ __forceinline__ void frame_c2c(const float2* __restrict__ src, float2
     stockham<L, C::LOG2R, INV, C::WARP>(v, t, tw, view);
     if (live) {
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) __stcs(dst + t + m * C::T, v[m]);
+        for (int m = 0; m < C::R; ++m) dst.st(t + m * C::T, v[m]);
     }
 }
 
-// Real forward: n = 2M reals (read as M packed pairs) -> M+1 complex bins (2 DFT).
-template <int LM>
-__device__ __forceinline__ void frame_r2c(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
+template <int L, bool INV>
+__device__ __forceinline__ void frame_c2c(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
                                           int t, const PaddedView& view, const float2* __restrict__ tw)
+{
+    frame_c2c_at<L, INV>(RowIn{src}, RowOut{dst}, live, t, view, tw);
+}
+
+// Real forward: n = 2M reals (read as M packed pairs) -> M+1 complex bins (2 DFT).
+template <int LM, class Src, class Dst>
+__device__ __forceinline__ void frame_r2c_at(const Src& src, const Dst& dst, bool live, int t,
+                                             const PaddedView& view, const float2* __restrict__ tw)
 {
     using C = SmallCfg<LM>;
     constexpr int M = 1 << LM;
     float2 v[C::R];
     if (live) {
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) v[m] = __ldcs(src + t + m * C::T);
+        for (int m = 0; m < C::R; ++m) v[m] = src.ld(t + m * C::T);
     } else {
 #pragma unroll
         for (int m = 0; m < C::R; ++m) v[m] = make_float2(0.f, 0.f);
@@ -114,10 +168,17 @@ __device__ __forceinline__ void frame_r2c(const float2* __restrict__ src, float2
     if (live) split_store<C, M>(view, dst, t, tw + 2 * M);
 }
 
-// Real inverse: M+1 complex bins -> n = 2M reals (written as M packed pairs).
 template <int LM>
-__device__ __forceinline__ void frame_c2r(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
+__device__ __forceinline__ void frame_r2c(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
                                           int t, const PaddedView& view, const float2* __restrict__ tw)
+{
+    frame_r2c_at<LM>(RowIn{src}, RowOut{dst}, live, t, view, tw);
+}
+
+// Real inverse: M+1 complex bins -> n = 2M reals (written as M packed pairs).
+template <int LM, class Src, class Dst>
+__device__ __forceinline__ void frame_c2r_at(const Src& src, const Dst& dst, bool live, int t,
+                                             const PaddedView& view, const float2* __restrict__ tw)
 {
     using C = SmallCfg<LM>;
     constexpr int M = 1 << LM;
@@ -129,8 +190,8 @@ __device__ __forceinline__ void frame_c2r(const float2* __restrict__ src, float2
         float2 a[C::R], b[C::R];
 #pragma unroll
         for (int m = 0; m < C::R; ++m) {
-            a[m] = __ldg(src + t + m * C::T);
-            b[m] = __ldg(src + (M - t - m * C::T));
+            a[m] = src.ldg(t + m * C::T);
+            b[m] = src.ldg(M - t - m * C::T);
         }
         const float2 w0 = __ldg(twn + t);
         static_for<0, C::R>([&](auto mc) {
@@ -144,8 +205,15 @@ __device__ __forceinline__ void frame_c2r(const float2* __restrict__ src, float2
     stockham<LM, C::LOG2R, true, C::WARP>(v, t, tw, view);
     if (live) {
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) __stcs(dst + t + m * C::T, v[m]);
+        for (int m = 0; m < C::R; ++m) dst.st(t + m * C::T, v[m]);
     }
+}
+
+template <int LM>
+__device__ __forceinline__ void frame_c2r(const float2* __restrict__ src, float2* __restrict__ dst, bool live,
+                                          int t, const PaddedView& view, const float2* __restrict__ tw)
+{
+    frame_c2r_at<LM>(RowIn{src}, RowOut{dst}, live, t, view, tw);
 }
 
 // ------------------------------------------------------------ batched kernels

@@ -26,6 +26,26 @@ constexpr int kSmallMaxLog2Real = 15;
 cudaError_t launch_small(Kind kind, int log2n, const void* in, void* out, long long count,
                          long long in_dist, long long out_dist, const float2* tw, cudaStream_t stream);
 
+// Advanced layout of a batch: element p of transform f is read from
+// in[f * in_dist + p * in_stride] and written to out[f * out_dist +
+// p * out_stride], in elements of each side's type (complex or float).
+struct Layout {
+    long long in_stride;
+    long long in_dist;
+    long long out_stride;
+    long long out_dist;
+};
+// Single-CTA sizes the strided kernels cover (complex 2^0..2^14, real 2^3..2^15).
+bool strided_supported(Kind kind, int log2n);
+cudaError_t launch_strided(Kind kind, int log2n, const void* in, void* out, long long count, const Layout& lay,
+                           const float2* tw, cudaStream_t stream);
+// `count` rows of `len` elements of `esize` bytes (4 or 8) between the
+// strided layout (stride, dist) and contiguous rows.
+cudaError_t launch_gather(const void* src, long long stride, long long dist, void* dst, long long count,
+                          long long len, int esize, cudaStream_t stream);
+cudaError_t launch_scatter(const void* src, void* dst, long long stride, long long dist, long long count,
+                           long long len, int esize, cudaStream_t stream);
+
 // Real transforms of n = 1, 2 or 4 points (closed forms, src/ckfft/fft_real.cpp:20-93).
 cudaError_t launch_real_tiny(Kind kind, int n, const void* in, void* out, long long count,
                              long long in_dist, long long out_dist, cudaStream_t stream);

@@ -103,8 +103,10 @@ const char* CkFftCudaGetLastError(void);
  * stream: a cudaStream_t passed as void*.  With NULL the call blocks until
  * `out` holds the results.  With a stream and device pointers for both `in`
  * and `out`, the work is only enqueued on that stream (asynchronous).  With a
- * host pointer on either side the call stages through device buffers,
- * pipelining copies against compute, and blocks.
+ * host pointer on either side the call blocks: page-locked host buffers of
+ * single-CTA sizes (complex n <= 2^14, real n <= 2^15) are read and written by
+ * the kernels in place; other host data is staged through device buffers,
+ * pipelining copies against compute.
  * Validation and return codes follow the single-transform calls; count == 0
  * is valid and does nothing; count < 0 returns 0. */
 int CkFftCudaComplexForwardBatch(CkFftContext* context, int n, int count,
@@ -115,6 +117,40 @@ int CkFftCudaRealForwardBatch(CkFftContext* context, int n, int count,
                               const float* input, CkFftComplex* output, void* stream);
 int CkFftCudaRealInverseBatch(CkFftContext* context, int n, int count,
                               const CkFftComplex* input, float* output, void* stream);
+
+/* Advanced-layout batches: element p of transform f is read from
+ * input[f * in_dist + p * in_stride] and written to
+ * output[f * out_dist + p * out_stride], in elements of each pointer's type
+ * (CkFftComplex or float).  Interleaved channels (stride = channels,
+ * dist = 1), columns of a row-major matrix (stride = row length, dist = 1),
+ * overlapping frames (stride = 1, dist = hop < n) and padded rows all run
+ * without a copy for complex n <= 2^14 and real 8 <= n <= 2^15; other sizes
+ * gather into contiguous rows and scatter back on the GPU.
+ *
+ * Rules: strides >= 1, distances >= 0 (in_dist == 0 transforms one input
+ * `count` times); the output transforms must not overlap one another (either
+ * out_dist >= (elements - 1) * out_stride + 1, or out_stride >= (count - 1) *
+ * out_dist + 1), and the input and output address ranges must not
+ * intersect.  Buffers are device, managed or page-locked host memory
+ * (pageable host memory returns 0).  stream: as for the Batch calls (NULL
+ * blocks; a stream with device buffers enqueues only).  Other validation and
+ * return codes follow the Batch calls. */
+int CkFftCudaComplexForwardStrided(CkFftContext* context, int n, long long count,
+                                   const CkFftComplex* input, long long in_stride, long long in_dist,
+                                   CkFftComplex* output, long long out_stride, long long out_dist,
+                                   void* stream);
+int CkFftCudaComplexInverseStrided(CkFftContext* context, int n, long long count,
+                                   const CkFftComplex* input, long long in_stride, long long in_dist,
+                                   CkFftComplex* output, long long out_stride, long long out_dist,
+                                   void* stream);
+int CkFftCudaRealForwardStrided(CkFftContext* context, int n, long long count,
+                                const float* input, long long in_stride, long long in_dist,
+                                CkFftComplex* output, long long out_stride, long long out_dist,
+                                void* stream);
+int CkFftCudaRealInverseStrided(CkFftContext* context, int n, long long count,
+                                const CkFftComplex* input, long long in_stride, long long in_dist,
+                                float* output, long long out_stride, long long out_dist,
+                                void* stream);
 
 /* Number of kernel launches the library has issued in this process (all
  * contexts, all threads).  Lets a caller count launches inside a timed region. */

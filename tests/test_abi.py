@@ -108,6 +108,10 @@ def test_transform_argument_checks_without_gpu(built):
     for f in (lib.CkFftCudaComplexForwardBatch, lib.CkFftCudaComplexInverseBatch,
               lib.CkFftCudaRealForwardBatch, lib.CkFftCudaRealInverseBatch):
         assert f(None, 8, 1, a, b, None) == 0
+    for f in (lib.CkFftCudaComplexForwardStrided, lib.CkFftCudaComplexInverseStrided,
+              lib.CkFftCudaRealForwardStrided, lib.CkFftCudaRealInverseStrided):
+        assert f(None, 8, 1, a, 1, 8, b, 1, 8, None) == 0
+        assert "context" in binding.last_error()
     lib.CkFftShutdown(None)
 
 
