@@ -26,11 +26,13 @@ class CkFftError(RuntimeError):
     """A CkFft call returned 0 / NULL; the message is CkFftCudaGetLastError()."""
 
 
-def header_functions() -> list[str]:
-    """Names of the functions declared in include/ckfft_cuda.h."""
-    text = open(HEADER).read()
+def header_functions(header: str | None = None, prefix: str = "CkFft") -> list[str]:
+    """Names of the functions declared in a public header (default
+    include/ckfft_cuda.h) that start with `prefix`."""
+    text = open(header or HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"\b(CkFft\w+)\s*\(", text)
+    text = "\n".join(l for l in text.splitlines() if not l.lstrip().startswith("#"))
+    names = re.findall(r"\b(" + prefix + r"\w*)\s*\(", text)
     seen = []
     for n in names:
         if n not in seen:
@@ -82,6 +84,25 @@ def _declare_extras(lib):
         if hasattr(lib, f):
             getattr(lib, f).restype = i
             getattr(lib, f).argtypes = [vp, i, ll, vp, ll, ll, vp, ll, ll, vp]
+    if hasattr(lib, "CkFftCudaStft"):
+        lib.CkFftCudaStft.restype = i
+        lib.CkFftCudaStft.argtypes = [vp, i, ll, vp, ll, ll, vp, C.c_float, vp, vp]
+        lib.CkFftCudaFilterInverse.restype = i
+        lib.CkFftCudaFilterInverse.argtypes = [vp, i, ll, vp, vp, C.c_float, vp, vp]
+    if hasattr(lib, "kiss_fft_alloc"):
+        for f in ("kiss_fft_alloc", "kiss_fftr_alloc"):
+            getattr(lib, f).restype = vp
+            getattr(lib, f).argtypes = [i, i, vp, C.POINTER(C.c_size_t)]
+        for f in ("kiss_fft", "kiss_fftr", "kiss_fftri"):
+            getattr(lib, f).restype = None
+            getattr(lib, f).argtypes = [vp, vp, vp]
+        lib.kiss_fft_stride.restype = None
+        lib.kiss_fft_stride.argtypes = [vp, vp, vp, i]
+        for f in ("kiss_fft_free", "kiss_fftr_free"):
+            getattr(lib, f).restype = None
+            getattr(lib, f).argtypes = [vp]
+        lib.kiss_fft_next_fast_size.restype = i
+        lib.kiss_fft_next_fast_size.argtypes = [i]
     if hasattr(lib, "CkFftCudaServerCreate"):
         lib.CkFftCudaServerCreate.restype = vp
         lib.CkFftCudaServerCreate.argtypes = [vp, C.c_size_t, i, ll]
@@ -224,6 +245,18 @@ class Context:
         }[kind]
         s = getattr(stream, "cuda_stream", stream)
         return fn(self.handle, n, count, ptr(inp), in_stride, in_dist, ptr(out), out_stride, out_dist, s)
+
+    def stft(self, n: int, frames: int, signal, hop: int, frame_len: int, window, scale: float, out,
+             stream=None) -> int:
+        """CkFftCudaStft: windowed frames at `hop` -> real forward x scale."""
+        s = getattr(stream, "cuda_stream", stream)
+        return self.lib.CkFftCudaStft(self.handle, n, frames, ptr(signal), hop, frame_len, ptr(window), scale,
+                                      ptr(out), s)
+
+    def filter_inverse(self, n: int, frames: int, spectra, filt, scale: float, out, stream=None) -> int:
+        """CkFftCudaFilterInverse: bins x filter x scale -> real inverse."""
+        s = getattr(stream, "cuda_stream", stream)
+        return self.lib.CkFftCudaFilterInverse(self.handle, n, frames, ptr(spectra), ptr(filt), scale, ptr(out), s)
 
     def run_jobs(self, jobs, stream=None) -> int:
         arr, n = job_array(jobs)

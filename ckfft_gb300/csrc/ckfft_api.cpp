@@ -599,6 +599,109 @@ int check_layout(const Work& w, const void* in, long long is, long long id, cons
     return 1;
 }
 
+// One buffer of a layout call: `span` bytes at `ptr`, read by the kernels
+// or (output) written by them.  `dev` is the address the kernels use.
+struct Span {
+    const void* ptr;
+    size_t span;
+    bool output;
+    void* dev;
+    bool staged;
+};
+
+constexpr size_t kStageLimit = 4ull << 30;
+
+// Runs body(stream) with every span addressable by the device.  Device and
+// managed memory and page-locked host ranges are used in place; pageable
+// host spans are staged through stream-ordered device memory (copied in
+// before the kernels -- outputs too, so that the gaps of a strided output
+// keep their contents -- and outputs copied back after; at most 4 GiB per
+// call).  stream != NULL with device spans only: asynchronous on that
+// stream.  Otherwise blocking on a lane stream ordered after the stream's
+// earlier work.
+template <class Body>
+int run_spans(CkFftContext* c, Span* sp, int nsp, void* stream, Body body)
+{
+    DeviceScope scope(c->device);
+    if (!scope.ok) return fail("cannot select the context's CUDA device");
+    bool all_dev = true, host_in = false;
+    size_t staged = 0;
+    for (int i = 0; i < nsp; ++i) {
+        sp[i].dev = (void*)sp[i].ptr;
+        sp[i].staged = false;
+        if (!sp[i].ptr || sp[i].span == 0) continue;
+        Mem m;
+        if (!classify(sp[i].ptr, c->device, &m)) return 0;
+        if (m == Mem::Device) continue;
+        all_dev = false;
+        if (mapped_range(sp[i].ptr, sp[i].span)) {
+            if (!sp[i].output) host_in = true;
+            continue;
+        }
+        sp[i].staged = true;
+        staged += (sp[i].span + 255) & ~(size_t)255;
+    }
+    if (staged > kStageLimit)
+        return fail("more than 4 GiB of pageable host memory in one call: use device or page-locked buffers");
+    const cudaStream_t us = (cudaStream_t)stream;
+    if (us && all_dev) {
+        const cudaError_t e = body(us);
+        return e == cudaSuccess ? 1 : cuda_fail("kernel launch", e);
+    }
+    Lane* lane = acquire_lane(c);
+    if (!lane) return fail("cannot create a staging lane (CUDA streams)");
+    const cudaStream_t s = lane->slot[0].stream;
+    cudaError_t e = cudaSuccess;
+    const char* where = "kernel launch";
+    cudaEvent_t dep = nullptr;
+    void* block = nullptr;
+    if (us) {
+        if ((e = cudaEventCreateWithFlags(&dep, cudaEventDisableTiming)) != cudaSuccess) where = "cudaEventCreate";
+        else if ((e = cudaEventRecord(dep, us)) != cudaSuccess) where = "cudaEventRecord";
+        else if ((e = cudaStreamWaitEvent(s, dep, 0)) != cudaSuccess) where = "cudaStreamWaitEvent";
+    }
+    if (e == cudaSuccess && staged) {
+        if ((e = ckg::pool_alloc_async(&block, staged, s)) != cudaSuccess) where = "stream-ordered staging allocation";
+        char* at = (char*)block;
+        for (int i = 0; i < nsp && e == cudaSuccess; ++i) {
+            if (!sp[i].staged) continue;
+            sp[i].dev = at;
+            at += (sp[i].span + 255) & ~(size_t)255;
+            if ((e = cudaMemcpyAsync(sp[i].dev, sp[i].ptr, sp[i].span, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+                where = "cudaMemcpyAsync(H2D)";
+        }
+    }
+    if (e == cudaSuccess) {
+        if (host_in) {
+            ckg::PlainLoadsScope plain;
+            e = body(s);
+        } else {
+            e = body(s);
+        }
+    }
+    for (int i = 0; i < nsp && e == cudaSuccess; ++i) {
+        if (!sp[i].staged || !sp[i].output) continue;
+        if ((e = cudaMemcpyAsync((void*)sp[i].ptr, sp[i].dev, sp[i].span, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            where = "cudaMemcpyAsync(D2H)";
+    }
+    if (block) cudaFreeAsync(block, s);
+    const cudaError_t se = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && se != cudaSuccess) { e = se; where = "cudaStreamSynchronize"; }
+    if (dep) cudaEventDestroy(dep);
+    release_lane(c, lane);
+    if (e != cudaSuccess) return cuda_fail(where, e);
+    if (ckg::take_device_error()) return fail("a kernel's bounded wait for its input copy timed out");
+    return 1;
+}
+
+// Byte ranges [a, a + na) and [b, b + nb) intersect (empty ranges never do).
+bool ranges_meet(const void* a, size_t na, const void* b, size_t nb)
+{
+    if (!a || !b || na == 0 || nb == 0) return false;
+    const uintptr_t a0 = (uintptr_t)a, b0 = (uintptr_t)b;
+    return a0 < b0 + nb && b0 < a0 + na;
+}
+
 int strided_call(CkFftContext* c, ckg::Kind kind, int n, long long count, const void* in, long long is,
                  long long id, void* out, long long os, long long od, void* stream)
 {
@@ -611,43 +714,68 @@ int strided_call(CkFftContext* c, ckg::Kind kind, int n, long long count, const 
     if (!check_layout(w, in, is, id, out, os, od, &in_span, &out_span)) return 0;
     w.in_dist = id;
     w.out_dist = od;
-    DeviceScope scope(c->device);
-    if (!scope.ok) return fail("cannot select the context's CUDA device");
-    Mem min, mout;
-    if (!classify(in, c->device, &min) || !classify(out, c->device, &mout)) return 0;
-    if ((min == Mem::Host && !mapped_range(in, in_span)) || (mout == Mem::Host && !mapped_range(out, out_span)))
-        return fail("strided batches need device, managed or page-locked host buffers covering the layout");
-    const cudaStream_t us = (cudaStream_t)stream;
-    if (us && min == Mem::Device && mout == Mem::Device) {
-        const cudaError_t e = enqueue_strided(c, w, in, is, out, os, us);
-        return e == cudaSuccess ? 1 : cuda_fail("kernel launch", e);
+    Span sp[2] = {{in, in_span, false, nullptr, false}, {out, out_span, true, nullptr, false}};
+    return run_spans(c, sp, 2, stream, [&](cudaStream_t s) {
+        return enqueue_strided(c, w, sp[0].dev, is, sp[1].dev, os, s);
+    });
+}
+
+// ------------------------------------------------------------ fused steps
+
+cudaError_t enqueue_stft(CkFftContext* c, int n, long long frames, const float* signal, long long hop,
+                         const float* window, long long frame_len, float scale, CkFftComplex* out, cudaStream_t s)
+{
+    const int log2n = log2i(n);
+    if (ckg::fused_supported(log2n))
+        return ckg::launch_stft(log2n, signal, hop, window, frame_len, scale, out, frames, c->dtw, s);
+    // windowed rows, contiguous real forward, then the scale
+    const long long bins = n / 2 + 1;
+    const Work all = make_work(ckg::R2C, n, frames);
+    long long g = (long long)((256ull << 20) / ((size_t)n * 4));
+    if (g < 1) g = 1;
+    if (g > frames) g = frames;
+    const size_t rows = ((size_t)g * n * 4 + 255) & ~(size_t)255;
+    const size_t large = scratch_need(all, g);
+    void* block = nullptr;
+    cudaError_t e = ckg::pool_alloc_async(&block, rows + large, s);
+    if (e != cudaSuccess) return e;
+    float* r = (float*)block;
+    void* tl = large ? (void*)((char*)block + rows) : nullptr;
+    for (long long off = 0; off < frames && e == cudaSuccess; off += g) {
+        const long long cnt = frames - off < g ? frames - off : g;
+        e = ckg::launch_window_rows(signal + off * hop, hop, window, frame_len, r, cnt, n, s);
+        if (e == cudaSuccess) e = enqueue(c, make_work(ckg::R2C, n, cnt), cnt, r, out + off * bins, tl, large, s);
+        if (e == cudaSuccess && scale != 1.0f) e = ckg::launch_scale_rows(out + off * bins, cnt * bins, scale, s);
     }
-    Lane* lane = acquire_lane(c);
-    if (!lane) return fail("cannot create a staging lane (CUDA streams)");
-    Slot& sl = lane->slot[0];
-    cudaError_t e = cudaSuccess;
-    const char* where = "kernel launch";
-    cudaEvent_t dep = nullptr;
-    if (us) {
-        if ((e = cudaEventCreateWithFlags(&dep, cudaEventDisableTiming)) != cudaSuccess) where = "cudaEventCreate";
-        else if ((e = cudaEventRecord(dep, us)) != cudaSuccess) where = "cudaEventRecord";
-        else if ((e = cudaStreamWaitEvent(sl.stream, dep, 0)) != cudaSuccess) where = "cudaStreamWaitEvent";
+    cudaFreeAsync(block, s);
+    return e;
+}
+
+cudaError_t enqueue_filter(CkFftContext* c, int n, long long frames, const CkFftComplex* spectra,
+                           const CkFftComplex* filter, float scale, float* out, cudaStream_t s)
+{
+    const int log2n = log2i(n);
+    if (ckg::fused_supported(log2n))
+        return ckg::launch_filter_inverse(log2n, spectra, filter, scale, out, frames, c->dtw, s);
+    // filtered rows, then the contiguous real inverse
+    const long long bins = n / 2 + 1;
+    const Work all = make_work(ckg::C2R, n, frames);
+    long long g = (long long)((256ull << 20) / ((size_t)bins * 8));
+    if (g < 1) g = 1;
+    if (g > frames) g = frames;
+    const size_t rows = ((size_t)g * bins * 8 + 255) & ~(size_t)255;
+    const size_t large = scratch_need(all, g);
+    void* block = nullptr;
+    cudaError_t e = ckg::pool_alloc_async(&block, rows + large, s);
+    if (e != cudaSuccess) return e;
+    void* tl = large ? (void*)((char*)block + rows) : nullptr;
+    for (long long off = 0; off < frames && e == cudaSuccess; off += g) {
+        const long long cnt = frames - off < g ? frames - off : g;
+        e = ckg::launch_filter_rows(spectra + off * bins, filter, scale, block, cnt, bins, s);
+        if (e == cudaSuccess) e = enqueue(c, make_work(ckg::C2R, n, cnt), cnt, block, out + off * n, tl, large, s);
     }
-    if (e == cudaSuccess) {
-        if (min == Mem::Host) {
-            ckg::PlainLoadsScope plain;
-            e = enqueue_strided(c, w, in, is, out, os, sl.stream);
-        } else {
-            e = enqueue_strided(c, w, in, is, out, os, sl.stream);
-        }
-    }
-    const cudaError_t se = cudaStreamSynchronize(sl.stream);
-    if (e == cudaSuccess && se != cudaSuccess) { e = se; where = "cudaStreamSynchronize"; }
-    if (dep) cudaEventDestroy(dep);
-    release_lane(c, lane);
-    if (e != cudaSuccess) return cuda_fail(where, e);
-    if (ckg::take_device_error()) return fail("a kernel's bounded wait for its input copy timed out");
-    return 1;
+    cudaFreeAsync(block, s);
+    return e;
 }
 
 int complex_call(CkFftContext* c, bool inverse, int n, long long count, const CkFftComplex* in,
@@ -834,6 +962,57 @@ int CkFftCudaRealInverseStrided(CkFftContext* c, int n, long long count, const C
                                 long long out_dist, void* stream)
 {
     return strided_call(c, ckg::C2R, n, count, in, in_stride, in_dist, out, out_stride, out_dist, stream);
+}
+
+int CkFftCudaStft(CkFftContext* c, int n, long long frames, const float* signal, long long hop,
+                  long long frame_len, const float* window, float scale, CkFftComplex* out, void* stream)
+{
+    if (!ctx_ok(c) || !has_fwd(c))
+        return fail(ctx_ok(c) ? "context was created without the forward direction" : "NULL or invalid context");
+    if (!valid_size(n, c->nmax)) return fail("n must be a power of two no larger than the context's nMax");
+    if (!signal || !out) return fail("signal and output must be non-NULL");
+    if (frames < 0 || frames > 0x7fffffffLL) return fail("frames must be in [0, 2^31)");
+    if (hop < 0) return fail("hop must be >= 0");
+    if (frame_len < 0 || frame_len > n) return fail("frame_len must be in [0, n]");
+    if ((uintptr_t)out & 7) return fail("output must be 8-byte aligned");
+    if (frames == 0) return 1;
+    const __int128 sig = frame_len ? ((__int128)(frames - 1) * hop + frame_len) * 4 : 0;
+    if (sig > ((__int128)1 << 62)) return fail("signal span too large");
+    const size_t s_sig = (size_t)sig, s_out = (size_t)frames * (size_t)(n / 2 + 1) * 8,
+                 s_win = window ? (size_t)n * 4 : 0;
+    if (ranges_meet(signal, s_sig, out, s_out) || ranges_meet(window, s_win, out, s_out))
+        return fail("input and output ranges overlap");
+    Span sp[3] = {{signal, s_sig, false, nullptr, false},
+                  {window, s_win, false, nullptr, false},
+                  {out, s_out, true, nullptr, false}};
+    return run_spans(c, sp, 3, stream, [&](cudaStream_t s) {
+        return enqueue_stft(c, n, frames, (const float*)sp[0].dev, hop, (const float*)sp[1].dev, frame_len, scale,
+                            (CkFftComplex*)sp[2].dev, s);
+    });
+}
+
+int CkFftCudaFilterInverse(CkFftContext* c, int n, long long frames, const CkFftComplex* spectra,
+                           const CkFftComplex* filter, float scale, float* out, void* stream)
+{
+    if (!ctx_ok(c) || !has_inv(c))
+        return fail(ctx_ok(c) ? "context was created without the inverse direction" : "NULL or invalid context");
+    if (!valid_size(n, c->nmax)) return fail("n must be a power of two no larger than the context's nMax");
+    if (!spectra || !out) return fail("spectra and output must be non-NULL");
+    if (frames < 0 || frames > 0x7fffffffLL) return fail("frames must be in [0, 2^31)");
+    if ((uintptr_t)out & 7) return fail("output must be 8-byte aligned");
+    if (frames == 0) return 1;
+    const size_t bins = (size_t)(n / 2 + 1);
+    const size_t s_in = (size_t)frames * bins * 8, s_out = (size_t)frames * (size_t)n * 4,
+                 s_f = filter ? bins * 8 : 0;
+    if (ranges_meet(spectra, s_in, out, s_out) || ranges_meet(filter, s_f, out, s_out))
+        return fail("input and output ranges overlap");
+    Span sp[3] = {{spectra, s_in, false, nullptr, false},
+                  {filter, s_f, false, nullptr, false},
+                  {out, s_out, true, nullptr, false}};
+    return run_spans(c, sp, 3, stream, [&](cudaStream_t s) {
+        return enqueue_filter(c, n, frames, (const CkFftComplex*)sp[0].dev, (const CkFftComplex*)sp[1].dev, scale,
+                              (float*)sp[2].dev, s);
+    });
 }
 
 long long CkFftCudaLaunchCount(void) { return ckg::launch_count(); }

@@ -46,6 +46,24 @@ cudaError_t launch_gather(const void* src, long long stride, long long dist, voi
 cudaError_t launch_scatter(const void* src, void* dst, long long stride, long long dist, long long count,
                            long long len, int esize, cudaStream_t stream);
 
+// Fused steps around the real transforms (single-CTA sizes, 8 <= n <= 2^15):
+// windowed frames at a hop -> real forward -> bins x scale; bins x filter x
+// scale -> real inverse.  `out` of launch_stft holds n/2+1 bins per frame,
+// `out` of launch_filter_inverse n reals per frame (8-byte aligned).
+bool fused_supported(int log2n);
+cudaError_t launch_stft(int log2n, const float* signal, long long hop, const float* window, long long frame_len,
+                        float scale, void* out, long long count, const float2* tw, cudaStream_t stream);
+cudaError_t launch_filter_inverse(int log2n, const void* spectra, const void* filter, float scale, float* out,
+                                  long long count, const float2* tw, cudaStream_t stream);
+// Row passes of the same steps for the other sizes: windowed frames into
+// contiguous rows of n reals; bins x filter x scale into contiguous rows;
+// `total` complex values scaled in place.
+cudaError_t launch_window_rows(const float* signal, long long hop, const float* window, long long frame_len,
+                               float* rows, long long count, long long n, cudaStream_t stream);
+cudaError_t launch_filter_rows(const void* spectra, const void* filter, float scale, void* rows, long long count,
+                               long long bins, cudaStream_t stream);
+cudaError_t launch_scale_rows(void* p, long long total, float scale, cudaStream_t stream);
+
 // Real transforms of n = 1, 2 or 4 points (closed forms, src/ckfft/fft_real.cpp:20-93).
 cudaError_t launch_real_tiny(Kind kind, int n, const void* in, void* out, long long count,
                              long long in_dist, long long out_dist, cudaStream_t stream);

@@ -131,10 +131,11 @@ int CkFftCudaRealInverseBatch(CkFftContext* context, int n, int count,
  * `count` times); the output transforms must not overlap one another (either
  * out_dist >= (elements - 1) * out_stride + 1, or out_stride >= (count - 1) *
  * out_dist + 1), and the input and output address ranges must not
- * intersect.  Buffers are device, managed or page-locked host memory
- * (pageable host memory returns 0).  stream: as for the Batch calls (NULL
- * blocks; a stream with device buffers enqueues only).  Other validation and
- * return codes follow the Batch calls. */
+ * intersect.  Buffers may be device, managed or page-locked host memory
+ * (used in place) or pageable host memory (the layout's whole span is staged
+ * through device memory, at most 4 GiB per call).  stream: as for the Batch
+ * calls (NULL blocks; a stream with device buffers enqueues only).  Other
+ * validation and return codes follow the Batch calls. */
 int CkFftCudaComplexForwardStrided(CkFftContext* context, int n, long long count,
                                    const CkFftComplex* input, long long in_stride, long long in_dist,
                                    CkFftComplex* output, long long out_stride, long long out_dist,
@@ -151,6 +152,28 @@ int CkFftCudaRealInverseStrided(CkFftContext* context, int n, long long count,
                                 const CkFftComplex* input, long long in_stride, long long in_dist,
                                 float* output, long long out_stride, long long out_dist,
                                 void* stream);
+
+/* Short-time Fourier transform: frame f (f < frames) is
+ * signal[f * hop + j] * window[j] for j < frame_len and 0 for frame_len <= j
+ * < n (window NULL: rectangular); its real forward transform (the scaling of
+ * CkFftRealForward) times `scale` is written as n/2+1 bins at
+ * output[f * (n/2+1)].  Overlapping frames (hop < n) and zero-padded frames
+ * (frame_len < n) read the signal once; window and scale cost no extra pass.
+ * signal must hold (frames - 1) * hop + frame_len floats; output 8-byte
+ * aligned and disjoint from signal and window.  Needs the forward direction.
+ * Buffers and stream as for the Strided calls.  Returns 1 or 0. */
+int CkFftCudaStft(CkFftContext* context, int n, long long frames, const float* signal, long long hop,
+                  long long frame_len, const float* window, float scale, CkFftComplex* output, void* stream);
+
+/* Spectral multiply + real inverse (FFT convolution / filtering): frame f's
+ * n/2+1 bins spectra[f * (n/2+1) + k] times filter[k] (one filter for every
+ * frame; NULL: none) times `scale`, real inverse transform (the scaling of
+ * CkFftRealInverse: round trip gain 2n), n reals at output[f * n].  Products
+ * are rounded one FP32 operation at a time.  output 8-byte aligned and
+ * disjoint from spectra and filter.  Needs the inverse direction.  Buffers
+ * and stream as for the Strided calls.  Returns 1 or 0. */
+int CkFftCudaFilterInverse(CkFftContext* context, int n, long long frames, const CkFftComplex* spectra,
+                           const CkFftComplex* filter, float scale, float* output, void* stream);
 
 /* Number of kernel launches the library has issued in this process (all
  * contexts, all threads).  Lets a caller count launches inside a timed region. */

@@ -31,6 +31,11 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def kiss_golden():
+    return np.load(os.path.join(ROOT, "tests", "golden", "kiss_golden.npz"))
+
+
+@pytest.fixture(scope="session")
 def oracle_mod():
     from oracle import oracle as orc
 

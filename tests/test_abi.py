@@ -43,6 +43,42 @@ def test_exports_every_declared_function(built):
         getattr(built, n)
 
 
+def test_exports_every_kiss_function(built):
+    """The kiss_fft-compatible boundary: every function of kiss_fft_cuda.h."""
+    names = binding.header_functions(os.path.join(ROOT, "include", "kiss_fft_cuda.h"), "kiss_")
+    assert {"kiss_fft_alloc", "kiss_fft", "kiss_fft_stride", "kiss_fft_free", "kiss_fft_cleanup",
+            "kiss_fft_next_fast_size", "kiss_fftr_alloc", "kiss_fftr", "kiss_fftri", "kiss_fftr_free"} == set(names)
+    out = subprocess.run(["nm", "-D", "--defined-only", LIB], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (\w+)", out))
+    assert not [n for n in names if n not in exported]
+
+
+def test_kiss_host_logic_without_gpu(built):
+    """Size query, size rules and NULL cfg, none of which needs a device."""
+    lib = built
+    lib.kiss_fft_alloc.restype = C.c_void_p
+    lib.kiss_fft_alloc.argtypes = [C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_size_t)]
+    lib.kiss_fftr_alloc.restype = C.c_void_p
+    lib.kiss_fftr_alloc.argtypes = [C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_size_t)]
+    lib.kiss_fft.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.kiss_fft_free.argtypes = [C.c_void_p]
+    n = C.c_size_t(0)
+    assert lib.kiss_fft_alloc(1024, 0, None, C.byref(n)) is None and n.value > 0
+    small = C.c_size_t(1)
+    buf = (C.c_char * 8)()
+    assert lib.kiss_fft_alloc(1024, 0, buf, C.byref(small)) is None and small.value == n.value
+    big = (C.c_char * 4096)()
+    assert lib.kiss_fft_alloc(1000, 0, big, C.byref(C.c_size_t(4096))) is None
+    assert "power of two" in binding.last_error()
+    assert lib.kiss_fftr_alloc(1, 0, None, None) is None
+    a, b = (C.c_float * 16)(), (C.c_float * 16)()
+    lib.kiss_fft(None, a, b)
+    assert "cfg" in binding.last_error()
+    lib.kiss_fft_free(None)
+    assert lib.kiss_fft_next_fast_size(1000) == 1024 and lib.kiss_fft_next_fast_size(1) == 1
+    assert lib.kiss_fft_next_fast_size(4096) == 4096
+
+
 def test_no_oracle_or_fallback_in_product():
     """The product library neither links nor names the oracle."""
     out = subprocess.run(["nm", "-D", LIB], capture_output=True, text=True, check=True).stdout
@@ -62,6 +98,18 @@ def test_header_compiles(tmp_path, std, lang):
     src = tmp_path / ("t.c" if lang == "c" else "t.cpp")
     src.write_text('#include "ckfft_cuda.h"\nint f(void) { CkFftComplex c; c.real = 1; c.imag = 2;'
                    ' return (int)(c.real + c.imag) + (int)kCkFftDirection_Both; }\n')
+    cc = "gcc" if lang == "c" else "g++"
+    subprocess.run([cc, f"-std={std}", "-pedantic", "-Wall", "-Werror", "-fsyntax-only",
+                    f"-I{os.path.join(ROOT, 'include')}", str(src)], check=True)
+
+
+@pytest.mark.parametrize("std,lang", [("c99", "c"), ("c++11", "c++")])
+def test_kiss_header_compiles(tmp_path, std, lang):
+    """kiss_fft_cuda.h compiles as C and C++, alone and with ckfft_cuda.h."""
+    src = tmp_path / ("k.c" if lang == "c" else "k.cpp")
+    src.write_text('#include "ckfft_cuda.h"\n#include "kiss_fft_cuda.h"\n'
+                   'int f(void) { kiss_fft_cpx c; c.r = 1; c.i = 2; kiss_fft_cfg g = 0; kiss_fftr_cfg h = 0;'
+                   ' (void)g; (void)h; return (int)(c.r + c.i) + kiss_fftr_next_fast_size_real(5); }\n')
     cc = "gcc" if lang == "c" else "g++"
     subprocess.run([cc, f"-std={std}", "-pedantic", "-Wall", "-Werror", "-fsyntax-only",
                     f"-I{os.path.join(ROOT, 'include')}", str(src)], check=True)

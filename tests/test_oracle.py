@@ -145,6 +145,39 @@ def test_kiss_third_opinion(oracle_mod, golden):
         assert np.sqrt(np.mean(np.concatenate([d.real, d.imag]) ** 2)) < 1e-3
 
 
+def test_kiss_fixtures(kiss_golden, oracle_mod):
+    """The kiss_fft fixtures are unscaled DFTs (FP64 check), kiss_fftri of
+    kiss_fftr is the round trip with gain n, and the oracle's real forward is
+    twice kiss_fftr (src/test/test.cpp:368-372) within the harness's RMS 1e-3."""
+    g = kiss_golden
+    for l2 in range(0, 12):
+        n = 1 << l2
+        x = g[f"cin_{l2}"].astype(np.complex128)
+        assert rel_l2(g[f"cfwd_{l2}"], np.fft.fft(x)) < 1e-6
+        assert rel_l2(g[f"cinv_{l2}"], np.fft.ifft(x) * n) < 1e-6
+        if l2 >= 1:
+            r = g[f"rin_{l2}"]
+            assert rel_l2(g[f"rfwd_{l2}"], np.fft.rfft(r.astype(np.float64))) < 1e-6
+            assert rel_l2(g[f"rinv_{l2}"], r * n) < 1e-6
+            o = oracle_mod.Oracle(max(n, 2))
+            d = o.real_forward(n, r) - 2 * g[f"rfwd_{l2}"]
+            assert np.sqrt(np.mean(np.abs(d) ** 2)) < 1e-3
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "oracle",
+                                                    "_ref", "libkissfft_ref.so")),
+                    reason="needs the reference's kiss_fft build (oracle/_ref)")
+def test_kiss_fixtures_regenerate(kiss_golden, oracle_mod):
+    """The committed kiss fixtures are kiss_fft's own outputs, bit for bit."""
+    k = oracle_mod.Kiss()
+    for l2 in (0, 3, 7, 11):
+        n = 1 << l2
+        assert same(k.complex(n, kiss_golden[f"cin_{l2}"]), kiss_golden[f"cfwd_{l2}"])
+        assert same(k.complex(n, kiss_golden[f"cin_{l2}"], True), kiss_golden[f"cinv_{l2}"])
+        if l2:
+            assert same(k.real_forward(n, kiss_golden[f"rin_{l2}"]), 2 * kiss_golden[f"rfwd_{l2}"])
+
+
 def test_batch_runner_matches_single(oracle_mod):
     rng = np.random.default_rng(5)
     n, frames = 256, 37

@@ -155,7 +155,19 @@ def test_layout_validation(torch_cuda, ctx_cache):
     assert ctx.strided("cfwd", 1000, 2, x, 1, 1024, y, 1, 1024) == 0        # not a power of two
     assert ctx.strided("cfwd", 1024, 0, x, 1, 1024, y, 1, 1024) == 1        # empty batch
     assert ctx.strided("cfwd", 1024, -1, x, 1, 1024, y, 1, 1024) == 0
-    pageable = np.zeros(1 << 12, np.complex64)
-    out = np.zeros(1 << 12, np.complex64)
-    assert ctx.strided("cfwd", 1024, 2, pageable, 1, 1024, out, 1, 1024) == 0
-    assert "page-locked" in binding.last_error()
+
+
+
+def test_pageable_host_layout_is_staged(torch_cuda, ctx_cache):
+    """Pageable buffers: the layout's spans are staged through device memory;
+    the gaps of a strided output keep their contents."""
+    ctx = ctx_cache(1024)
+    rng = np.random.default_rng(8)
+    x = (rng.uniform(-1, 1, 4 * 1024) + 1j * rng.uniform(-1, 1, 4 * 1024)).astype(np.complex64)
+    out = np.full(8 * 1024, 7 + 7j, np.complex64)
+    ctx.check(ctx.strided("cfwd", 1024, 4, x, 4, 1, out, 2, 2048))
+    xd = torch_cuda.from_numpy(x).cuda()
+    yd = torch_cuda.full((8 * 1024,), 7 + 7j, dtype=torch_cuda.complex64, device="cuda")
+    ctx.check(ctx.strided("cfwd", 1024, 4, xd, 4, 1, yd, 2, 2048))
+    assert np.array_equal(bits(out), bits(yd.cpu().numpy()))
+    assert np.all(out[1::2] == 7 + 7j)
