@@ -540,6 +540,11 @@ cudaError_t enqueue_strided(CkFftContext* c, const Work& w, const void* in, long
         if (scratch) cudaFreeAsync(scratch, s);
         return e;
     }
+    // consecutive transforms adjacent (interleaved channels, matrix columns)
+    const bool cin = w.in_dist == 1 && is > 1, cout = w.out_dist == 1 && os > 1;
+    if (ckg::inter_applies(w.kind, w.log2n, cin, cout))
+        return ckg::launch_inter(w.kind, w.log2n, in, out, w.count, ckg::Layout{is, w.in_dist, os, w.out_dist}, cin,
+                                 cout, c->dtw, s);
     if (ckg::strided_supported(w.kind, w.log2n))
         return ckg::launch_strided(w.kind, w.log2n, in, out, w.count, ckg::Layout{is, w.in_dist, os, w.out_dist},
                                    c->dtw, s);

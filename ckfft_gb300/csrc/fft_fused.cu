@@ -9,12 +9,16 @@
 // Sizes outside the single-CTA range form the products in a row pass
 // (k_window_rows / k_filter_rows) ahead of the contiguous path, and the
 // forward scale in k_scale_rows after it.
+#include <cstdint>
+
 #include "fft_small.cuh"
 
 namespace ckg {
 
-// Reals of one frame, windowed, zero past `len`, as packed pairs.
-template <bool WIN>
+// Reals of one frame, windowed, zero past `len`, as packed pairs.  VEC:
+// whole frames (len == n) whose start and window sit on 8-byte boundaries,
+// both read as pairs.
+template <bool WIN, bool VEC>
 struct WindowIn {
     const float* __restrict__ x;
     const float* __restrict__ w;
@@ -22,9 +26,20 @@ struct WindowIn {
     __device__ __forceinline__ float2 ld(long long i) const
     {
         const long long j = 2 * i;
-        float a = j < len ? __ldg(x + j) : 0.f;
-        float b = j + 1 < len ? __ldg(x + j + 1) : 0.f;
-        if constexpr (WIN) {
+        float a, b;
+        if constexpr (VEC) {
+            const float2 v = __ldcs(reinterpret_cast<const float2*>(x) + i);
+            a = v.x;
+            b = v.y;
+        } else {
+            a = j < len ? __ldg(x + j) : 0.f;
+            b = j + 1 < len ? __ldg(x + j + 1) : 0.f;
+        }
+        if constexpr (WIN && VEC) {
+            const float2 u = __ldg(reinterpret_cast<const float2*>(w) + i);
+            a = __fmul_rn(a, u.x);
+            b = __fmul_rn(b, u.y);
+        } else if constexpr (WIN) {
             a = __fmul_rn(a, __ldg(w + j));
             b = __fmul_rn(b, __ldg(w + j + 1));
         }
@@ -64,7 +79,7 @@ struct FilterIn {
     __device__ __forceinline__ float2 ldg(long long i) const { return ld(i); }
 };
 
-template <int LM, bool WIN>
+template <int LM, bool WIN, bool VEC>
 __global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
 k_stft(const float* __restrict__ signal, long long hop, const float* __restrict__ window, long long frame_len,
        float scale, float2* __restrict__ out, long long count, const float2* __restrict__ tw)
@@ -75,7 +90,7 @@ k_stft(const float* __restrict__ signal, long long hop, const float* __restrict_
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
     const long long f = (long long)blockIdx.x * C::TPB + g;
     const long long fc = f < count ? f : 0;
-    frame_r2c_at<LM>(WindowIn<WIN>{signal + fc * hop, window, frame_len}, ScaledOut{out + fc * (M + 1), scale},
+    frame_r2c_at<LM>(WindowIn<WIN, VEC>{signal + fc * hop, window, frame_len}, ScaledOut{out + fc * (M + 1), scale},
                      f < count, t, PaddedView{smem + g * C::SLOT}, tw);
 }
 
@@ -137,10 +152,18 @@ static cudaError_t launch_stft_L(const float* signal, long long hop, const float
 {
     using C = SmallCfg<LM>;
     const unsigned grid = (unsigned)((count + C::TPB - 1) / C::TPB);
-    if (window)
-        k_stft<LM, true><<<grid, C::THREADS, C::SMEM, s>>>(signal, hop, window, frame_len, scale, out, count, tw);
-    else
-        k_stft<LM, false><<<grid, C::THREADS, C::SMEM, s>>>(signal, hop, window, frame_len, scale, out, count, tw);
+    const bool vec = frame_len == (2ll << LM) && hop % 2 == 0 && ((uintptr_t)signal & 7) == 0 &&
+                     ((uintptr_t)window & 7) == 0;
+#define CKG_STFT(W, V) \
+    k_stft<LM, W, V><<<grid, C::THREADS, C::SMEM, s>>>(signal, hop, window, frame_len, scale, out, count, tw)
+    if (window) {
+        if (vec) CKG_STFT(true, true);
+        else CKG_STFT(true, false);
+    } else {
+        if (vec) CKG_STFT(false, true);
+        else CKG_STFT(false, false);
+    }
+#undef CKG_STFT
     return cudaGetLastError();
 }
 
@@ -240,8 +263,10 @@ template <int LM>
 static cudaError_t attr_fused()
 {
     const int smem = (int)SmallCfg<LM>::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k_stft<LM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_stft<LM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(k_stft<LM, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_stft<LM, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_stft<LM, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_stft<LM, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_filter_c2r<LM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_filter_c2r<LM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     return e;

@@ -176,14 +176,14 @@ __device__ __forceinline__ void frame_r2c(const float2* __restrict__ src, float2
 }
 
 // Real inverse: M+1 complex bins -> n = 2M reals (written as M packed pairs).
-template <int LM, class Src, class Dst>
-__device__ __forceinline__ void frame_c2r_at(const Src& src, const Dst& dst, bool live, int t,
-                                             const PaddedView& view, const float2* __restrict__ tw)
+// The real inverse's first step: v[m] = merge(X[p], X[M-p]) at p = t + mT.
+template <int LM, class Src>
+__device__ __forceinline__ void c2r_load(const Src& src, bool live, int t, const float2* __restrict__ tw,
+                                         float2 (&v)[SmallCfg<LM>::R])
 {
     using C = SmallCfg<LM>;
     constexpr int M = 1 << LM;
     const float2* twn = tw + 2 * M;
-    float2 v[C::R];
     if (live) {
         // both merge operands straight from HBM: X[p] coalesced ascending and
         // X[M-p] coalesced descending (the second read of each line hits cache)
@@ -202,6 +202,15 @@ __device__ __forceinline__ void frame_c2r_at(const Src& src, const Dst& dst, boo
 #pragma unroll
         for (int m = 0; m < C::R; ++m) v[m] = make_float2(0.f, 0.f);
     }
+}
+
+template <int LM, class Src, class Dst>
+__device__ __forceinline__ void frame_c2r_at(const Src& src, const Dst& dst, bool live, int t,
+                                             const PaddedView& view, const float2* __restrict__ tw)
+{
+    using C = SmallCfg<LM>;
+    float2 v[C::R];
+    c2r_load<LM>(src, live, t, tw, v);
     stockham<LM, C::LOG2R, true, C::WARP>(v, t, tw, view);
     if (live) {
 #pragma unroll

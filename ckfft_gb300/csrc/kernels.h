@@ -39,6 +39,13 @@ struct Layout {
 bool strided_supported(Kind kind, int log2n);
 cudaError_t launch_strided(Kind kind, int log2n, const void* in, void* out, long long count, const Layout& lay,
                            const float2* tw, cudaStream_t stream);
+// Layouts whose consecutive transforms are adjacent (distance 1, stride > 1)
+// on the input (cin) and / or output (cout) side: CTAs move whole rows of
+// consecutive transforms (fft_inter.cu).  Complex 2^6..2^13 with cin or
+// cout; real forward with cin, real inverse with cout, n = 2^7..2^14.
+bool inter_applies(Kind kind, int log2n, bool cin, bool cout);
+cudaError_t launch_inter(Kind kind, int log2n, const void* in, void* out, long long count, const Layout& lay,
+                         bool cin, bool cout, const float2* tw, cudaStream_t stream);
 // `count` rows of `len` elements of `esize` bytes (4 or 8) between the
 // strided layout (stride, dist) and contiguous rows.
 cudaError_t launch_gather(const void* src, long long stride, long long dist, void* dst, long long count,

@@ -80,6 +80,16 @@ LAYOUTS = [
     ("real-8", "rinv", 8, 100, 2, 11, 1, 8),
     ("real-2^15-columns", "rfwd", 1 << 15, 3, 3, 1, 1, (1 << 14) + 1),
     ("complex-2^14-stride", "cfwd", 1 << 14, 3, 2, 1 << 15, 1, 1 << 14),
+    # consecutive transforms adjacent (distance 1): CTAs move whole rows
+    ("inter-2^13-both", "cfwd", 1 << 13, 5, 5, 1, 5, 1),
+    ("inter-2^12-in", "cinv", 1 << 12, 7, 9, 1, 1, 1 << 12),
+    ("inter-2^11-out", "cfwd", 1 << 11, 3, 1, 1 << 11, 3, 1),
+    ("inter-64-both", "cinv", 64, 100, 100, 1, 101, 1),
+    ("inter-real-2^14-in", "rfwd", 1 << 14, 3, 3, 1, 1, (1 << 13) + 1),
+    ("inter-real-2^14-out", "rinv", 1 << 14, 5, 1, (1 << 13) + 1, 5, 1),
+    ("inter-real-128-in", "rfwd", 128, 70, 70, 1, 2, 130),
+    ("inter-real-128-out", "rinv", 128, 65, 1, 65, 65, 1),
+    ("inter-real-4096-in-out-strided", "rfwd", 4096, 9, 9, 1, 9, 1),
 ]
 
 
