@@ -96,7 +96,26 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     if ptxas_info:
         for o in outputs:
             sys.stdout.write(o)
+    build_harness(nvcc, headers, force, verbose)
     return LIB
+
+
+HARNESS_SRC = os.path.join(HERE, "harness", "ckfft_timing.cpp")
+HARNESS = os.path.join(BUILD, "ckfft_timing")
+
+
+def build_harness(nvcc: str, headers, force: bool = False, verbose: bool = False) -> str:
+    """The timing harness executable (_build/ckfft_timing), linked against
+    the library in this directory and the CUDA runtime."""
+    if not force and not _stale(HARNESS, [HARNESS_SRC, LIB] + headers):
+        return HARNESS
+    cuda = os.path.dirname(_cuda_include(nvcc))
+    lib64 = os.path.join(cuda, "lib64")
+    cxx = os.environ.get("CXX", "g++")
+    _run([cxx, "-O2", "-std=c++17", "-Wall", f"-I{INCLUDE}", f"-I{_cuda_include(nvcc)}", HARNESS_SRC,
+          "-o", HARNESS, f"-L{HERE}", "-l:libckfft_cuda.so", f"-L{lib64}", "-lcudart",
+          "-Wl,-rpath,$ORIGIN/..", f"-Wl,-rpath,{lib64}"], verbose)
+    return HARNESS
 
 
 def main():
