@@ -19,6 +19,7 @@ cudaError_t prepare_cluster();
 cudaError_t prepare_strided();
 cudaError_t prepare_fused();
 cudaError_t prepare_inter();
+cudaError_t prepare_l2pass();
 
 // Opt-in (CKFFT_CUDA_CLUSTER=1): measured slower than the default paths on
 // GB300 (2^14: 2366 vs 3669 GB/s single CTA; 2^15 / 2^16: 1936 / 1516 vs about
@@ -164,6 +165,7 @@ cudaError_t prepare_device()
     if ((e = prepare_strided()) != cudaSuccess) return e;
     if ((e = prepare_fused()) != cudaSuccess) return e;
     if ((e = prepare_inter()) != cudaSuccess) return e;
+    if ((e = prepare_l2pass()) != cudaSuccess) return e;
     if (dev < 64) done |= 1ull << dev;
     return cudaSuccess;
 }

@@ -1,0 +1,143 @@
+// fft_l2pass.cu -- complex 2^15 and 2^16 in two passes whose intermediate
+// never reaches HBM.
+//
+// The multi-pass transform of fft_large.cu (columns, then rows, see
+// fft_passes.cuh) runs here inside one thread-block cluster of K CTAs per
+// transform: the cluster's CTAs share the column tiles, meet at a cluster
+// barrier (release / acquire at cluster scope), share the row tiles, and each
+// row tile's CTA drops the intermediate's L2 lines once it has read them.
+// The intermediate of the transforms in flight (resident clusters x 8n
+// bytes, 19 / 38 MB here) stays in the 129 MB L2, so HBM sees the input read
+// once and the output written once -- the traffic of a single pass -- while
+// the batched two-pass kernels move every value through HBM twice.  Measured
+// on GB300 (batches of 1 GiB): 2^15 3328 vs 3145 GB/s, 2^16 3439 vs 3105;
+// the kernel is then bound by the two passes' instructions, not by HBM (40 %
+// DRAM throughput, no intermediate bytes in DRAM).  At 2^17 it was slower
+// (2779 vs 2857) and is not used there.
+#include <cooperative_groups.h>
+
+#include "fft_passes.cuh"
+#include "kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace ckg {
+
+constexpr int kL2Threads = 256;
+constexpr int kL2Cluster = 8;
+
+template <int LA, int LB>
+struct L2Cfg {
+    using PA = PassCfg<LA, kL2Threads>;
+    using PB = PassCfg<LB, kL2Threads>;
+    static constexpr int SGA = kL2Threads / PA::THREADS;     // column tiles at once
+    static constexpr int SGB = kL2Threads / PB::THREADS;     // row tiles at once
+    static constexpr int TILES_A = (1 << LB) / PA::C;        // column tiles of one transform
+    static constexpr int TILES_B = (1 << LA) / PB::C;        // row tiles
+    static constexpr int ITER_A = TILES_A / (kL2Cluster * SGA);
+    static constexpr int ITER_B = TILES_B / (kL2Cluster * SGB);
+    static constexpr size_t SMEM_A = PA::SMEM * SGA, SMEM_B = PB::SMEM * SGB;
+    static constexpr size_t SMEM = SMEM_A > SMEM_B ? SMEM_A : SMEM_B;
+    static_assert(PA::THREADS * SGA == kL2Threads && PB::THREADS * SGB == kL2Threads, "whole CTAs per phase");
+    static_assert(ITER_A >= 1 && ITER_A * kL2Cluster * SGA == TILES_A, "column tiles split evenly");
+    static_assert(ITER_B >= 1 && ITER_B * kL2Cluster * SGB == TILES_B, "row tiles split evenly");
+};
+
+// One transform per cluster: blockIdx.x / K.  scratch holds n values per
+// transform of the launch (128-byte aligned rows).
+template <int LA, int LB, bool INV>
+__global__ void __cluster_dims__(kL2Cluster, 1, 1) __launch_bounds__(kL2Threads, 4)
+k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __restrict__ scratch, long long in_dist,
+         long long out_dist, const float2* __restrict__ tw)
+{
+    using C = L2Cfg<LA, LB>;
+    constexpr long long n = 1ll << (LA + LB);
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const long long f = blockIdx.x / kL2Cluster;
+    extern __shared__ __align__(128) float2 smem[];
+    const float2* x = in + f * in_dist;
+    float2* y = out + f * out_dist;
+    float2* s = scratch + f * n;
+
+    const int sga = threadIdx.x / C::PA::THREADS, ta = threadIdx.x % C::PA::THREADS;
+#pragma unroll 1
+    for (int i = 0; i < C::ITER_A; ++i) {
+        const int tile = (i * kL2Cluster + rank) * C::SGA + sga;
+        pass_cols<LA, INV, false, kL2Threads>(x, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
+        __syncthreads();                             // the tile's shared memory is reused
+    }
+    // every column tile of the transform is in L2 before any row tile reads
+    // it: the cluster barrier releases and acquires at cluster scope; the
+    // fence makes the ordering of the global stores explicit
+    asm volatile("fence.acq_rel.cluster;" ::: "memory");
+    cluster.sync();
+    const int sgb = threadIdx.x / C::PB::THREADS, tb = threadIdx.x % C::PB::THREADS;
+#pragma unroll 1
+    for (int i = 0; i < C::ITER_B; ++i) {
+        const int tile = (i * kL2Cluster + rank) * C::SGB + sgb;
+        pass_rows<LB, INV, true, kL2Threads, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, tw);
+        __syncthreads();
+    }
+}
+
+template <int LA, int LB, bool INV>
+static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, long long count, long long in_dist,
+                               long long out_dist, const float2* tw, cudaStream_t s)
+{
+    using C = L2Cfg<LA, LB>;
+    k_l2_c2c<LA, LB, INV><<<(unsigned)(count * kL2Cluster), kL2Threads, C::SMEM, s>>>(in, out, scratch, in_dist,
+                                                                                    out_dist, tw);
+    return cudaGetLastError();
+}
+
+bool l2pass_supported(int log2n) { return log2n >= 15 && log2n <= 16; }
+
+cudaError_t launch_l2pass_c2c(bool inverse, int log2n, const void* in, void* out, long long count, long long in_dist,
+                              long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes,
+                              cudaStream_t s)
+{
+    if (!l2pass_supported(log2n)) return cudaErrorInvalidValue;
+    if (count <= 0) return cudaSuccess;
+    const long long n = 1ll << log2n;
+    const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
+    if (group < 1 || ((uintptr_t)scratch & 127)) return cudaErrorInvalidValue;
+    const float2* src = (const float2*)in;
+    float2* dst = (float2*)out;
+    float2* tmp = (float2*)scratch;
+    for (long long off = 0; off < count; off += group) {
+        const long long cnt = count - off < group ? count - off : group;
+        const float2* a = src + off * in_dist;
+        float2* b = dst + off * out_dist;
+        cudaError_t e;
+        switch (log2n) {
+        case 15: e = inverse ? launch_l2_L<7, 8, true>(a, b, tmp, cnt, in_dist, out_dist, tw, s)
+                             : launch_l2_L<7, 8, false>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;
+        case 16: e = inverse ? launch_l2_L<8, 8, true>(a, b, tmp, cnt, in_dist, out_dist, tw, s)
+                             : launch_l2_L<8, 8, false>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;
+        default: e = cudaErrorInvalidValue;
+        }
+        if (e != cudaSuccess) return e;
+        count_launch();
+    }
+    return cudaSuccess;
+}
+
+template <int LA, int LB>
+static cudaError_t attr_l2()
+{
+    const int smem = (int)L2Cfg<LA, LB>::SMEM;
+    cudaError_t e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return e;
+}
+
+cudaError_t prepare_l2pass()
+{
+    cudaError_t e = attr_l2<7, 8>();
+    if (e == cudaSuccess) e = attr_l2<8, 8>();
+    return e;
+}
+
+}  // namespace ckg

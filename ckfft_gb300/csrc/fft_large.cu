@@ -13,6 +13,8 @@
 // rows (pass 2) per CTA so every warp access covers C*8 contiguous bytes.
 // Real sizes run the half-length complex transform plus a split (forward) or
 // merge (inverse) pass, the algebra of src/ckfft/fft_real_default.cpp.
+#include <cstdint>
+
 #include "fft_passes.cuh"
 #include "kernels.h"
 
@@ -158,6 +160,10 @@ cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out,
 {
     if (!large_supported(log2n)) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;
+    // 2^15, 2^16: both passes inside one cluster per transform, the
+    // intermediate kept in L2 (fft_l2pass.cu)
+    if (l2pass_supported(log2n) && ((uintptr_t)scratch & 127) == 0)
+        return launch_l2pass_c2c(inverse, log2n, in, out, count, in_dist, out_dist, tw, scratch, scratch_bytes, s);
     const LargePlan p = large_plan(log2n);
     const long long n = 1ll << log2n;
     const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));

@@ -67,9 +67,12 @@ __device__ __forceinline__ float2 big_twiddle(const float2* __restrict__ tw, int
 }
 
 // Column pass for tile `tile` of one transform, by threads tid = 0..THREADS-1.
+// live == false: the threads take part in the barriers only (no memory
+// access outside the tile's shared memory).
 template <int LA, bool INV, bool CG, int MAXT = 512>
 __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
-                                          long long tile, int tid, float2* smem, const float2* __restrict__ tw)
+                                          long long tile, int tid, float2* smem, const float2* __restrict__ tw,
+                                          bool live = true)
 {
     using P = PassCfg<LA, MAXT>;
     const int c = tid % P::C, t = tid / P::C;
@@ -78,7 +81,8 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
     const float2* src = in + n2;
     float2 v[P::R];
 #pragma unroll
-    for (int m = 0; m < P::R; ++m) v[m] = ld_data<CG>(src + (long long)(t + m * P::T) * n2len);
+    for (int m = 0; m < P::R; ++m)
+        v[m] = live ? ld_data<CG>(src + (long long)(t + m * P::T) * n2len) : make_float2(0.f, 0.f);
     TileView<P::C> view{smem, c};
     stockham<LA, P::LOG2R, INV, false>(v, t, tw, view);
     const int ln = LA + log2n2;
@@ -96,6 +100,7 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
     float2 ladder[Q > 1 ? ilog2(Q) : 1];
 #pragma unroll
     for (int i = 0; (1 << i) < Q; ++i) ladder[i] = big_twiddle<INV>(tw, ln, (int)(((long long)pT << (2 + i)) & mask));
+    if (!live) return;
     static_for<0, Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
         float2 aq = a;
@@ -115,7 +120,8 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
 // dropped without write-back once read; it must be 128-byte aligned.
 template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true>
 __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
-                                          long long tile, int tid, float2* smem, const float2* __restrict__ tw)
+                                          long long tile, int tid, float2* smem, const float2* __restrict__ tw,
+                                          bool live = true)
 {
     using P = PassCfg<LB, MAXT>;
     constexpr int N2 = 1 << LB;
@@ -125,11 +131,11 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
     const float2* src = in + (row0 + r) * N2 + t;
     float2 v[P::R];
 #pragma unroll
-    for (int m = 0; m < P::R; ++m) v[m] = ld_data<CG>(src + m * P::T);
+    for (int m = 0; m < P::R; ++m) v[m] = live ? ld_data<CG>(src + m * P::T) : make_float2(0.f, 0.f);
     PaddedView view{smem + r * padded_len(N2)};
     stockham<LB, P::LOG2R, INV, (P::T <= 32)>(v, t, tw, view);
     __syncthreads();
-    if constexpr (DISCARD) {
+    if (DISCARD && live) {
         // every thread of the tile has consumed its inputs: the intermediate
         // rows are dead, so drop their L2 lines instead of writing them back
         static_assert(N2 % 16 == 0, "rows span whole 128-byte lines");
@@ -144,6 +150,7 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
     __syncthreads();
     const int r2 = tid % P::C, t2 = tid / P::C;
     float2* dst = out + row0 + r2;
+    if (!live) return;
 #pragma unroll
     for (int m = 0; m < P::R; ++m) {
         const int k2 = t2 + m * P::T;

@@ -103,6 +103,14 @@ bool cluster_enabled();
 cudaError_t launch_cluster_c2c(bool inverse, int log2n, const void* in, void* out, long long count,
                                long long in_dist, long long out_dist, const float2* tw, cudaStream_t stream);
 
+// Complex 2^15 and 2^16 with both passes inside one thread-block cluster per
+// transform and the intermediate kept in L2 (fft_l2pass.cu); scratch as for
+// launch_large_c2c, 128-byte aligned.
+bool l2pass_supported(int log2n);
+cudaError_t launch_l2pass_c2c(bool inverse, int log2n, const void* in, void* out, long long count, long long in_dist,
+                              long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes,
+                              cudaStream_t stream);
+
 // Scratch bytes one transform of the given kind and size needs on the large path.
 size_t large_scratch_bytes(Kind kind, int log2n);
 

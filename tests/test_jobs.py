@@ -80,6 +80,34 @@ def test_same_alone_and_in_the_mix(torch_cuda, ctx_cache):
                                 else torch_cuda.view_as_real(m).view(torch_cuda.int32)), (j["kind"], j["n"])
 
 
+def test_run_up_to_2e17(torch_cuda, ctx_cache, oracle_mod):
+    """Every kind and size up to complex 2^17 / real 2^18 in one run: oracle
+    parity, and the same bits as each job run alone."""
+    torch = torch_cuda
+    rng = np.random.default_rng(7)
+    jobs = []
+    for kind in ("cfwd", "cinv"):
+        for l2 in range(0, 18):
+            jobs.append(make_job(torch, rng, kind, 1 << l2, 3 if l2 <= 14 else 2))
+    for kind in ("rfwd", "rinv"):
+        for l2 in range(0, 19):
+            jobs.append(make_job(torch, rng, kind, 1 << l2, 3 if l2 <= 15 else 2))
+    jobs = [jobs[i] for i in rng.permutation(len(jobs))]
+    ctx = ctx_cache(1 << 18)
+    ctx.check(ctx.run_jobs([as_tuple(j) for j in jobs]), "mixed run")
+    o = oracle_mod.Oracle(1 << 18)
+    mixed = [j["out"].clone() for j in jobs]
+    for j, m in zip(jobs, mixed):
+        got = m.cpu().numpy()
+        for f in range(j["count"]):
+            assert_close(got[f], oracle_out(o, j, f), j["n"], f"mixed {j['kind']} n={j['n']} frame {f}")
+        j["out"].fill_(float("nan"))
+        ctx.check(ctx.run_jobs([as_tuple(j)]), "alone")
+        a = j["out"].view(torch.int32) if j["out"].dtype == torch.float32 else torch.view_as_real(j["out"]).view(torch.int32)
+        b = m.view(torch.int32) if m.dtype == torch.float32 else torch.view_as_real(m).view(torch.int32)
+        assert torch.equal(a, b), (j["kind"], j["n"])
+
+
 def test_plan_replays_and_reads_current_inputs(torch_cuda, ctx_cache, oracle_mod):
     torch = torch_cuda
     rng = np.random.default_rng(2)
