@@ -39,13 +39,13 @@ __device__ __forceinline__ bool wait_counter(const int* p, int need, unsigned* e
 // ----------------------------------------------------------- unit bodies
 
 template <int OP, int L>
-__device__ __noinline__ void run_single(const Unit& u, const JobsArgs& a, float2* smem)
+__device__ __noinline__ void run_single(const UnitRec& r, const JobsArgs& a, float2* smem)
 {
     using C = SmallCfg<L>;
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
-    const bool live = g < u.count;
+    const bool live = g < r.u.count;
     FrameDesc fd{nullptr, nullptr};
-    if (live) fd = a.frames[u.first + g];
+    if (live) fd = r.frames[g];
     const PaddedView view{smem + g * C::SLOT};
     if constexpr (OP == U_C2C_FWD) frame_c2c<L, false>(fd.in, fd.out, live, t, view, a.tw);
     else if constexpr (OP == U_C2C_INV) frame_c2c<L, true>(fd.in, fd.out, live, t, view, a.tw);
@@ -54,12 +54,12 @@ __device__ __noinline__ void run_single(const Unit& u, const JobsArgs& a, float2
 }
 
 // Real n = 1, 2, 4 closed forms (src/ckfft/fft_real.cpp:20-93), one frame per thread.
-__device__ __noinline__ void run_rtiny(const Unit& u, const JobsArgs& a, bool inv)
+__device__ __noinline__ void run_rtiny(const UnitRec& r, bool inv)
 {
     const int g = threadIdx.x;
-    if (g >= u.count) return;
-    const FrameDesc fd = a.frames[u.first + g];
-    const int n = 1 << u.log2a;
+    if (g >= r.u.count) return;
+    const FrameDesc fd = r.frames[g];
+    const int n = 1 << r.u.log2a;
     if (!inv) {
         const float* x = (const float*)fd.in;
         float2* y = fd.out;
@@ -101,11 +101,12 @@ __device__ __forceinline__ float2* pick(const LargeDesc& d, int sel)
 
 // A pass unit carries kJobThreads / THREADS whole tiles, one per subgroup.
 template <int OP, int LS>
-__device__ __noinline__ void run_pass(const Unit& u, const JobsArgs& a, float2* smem)
+__device__ __noinline__ void run_pass(const UnitRec& r, const JobsArgs& a, float2* smem)
 {
     using P = PassCfg<LS, kJobThreads>;
+    const Unit& u = r.u;
     const int s = threadIdx.x / P::THREADS, tid = threadIdx.x % P::THREADS;
-    const LargeDesc d = a.large[u.job];
+    const LargeDesc d = r.big;
     const float2* src = pick(d, u.sel & 15);
     float2* dst = pick(d, u.sel >> 4);
     float2* my = smem + s * P::SLOTS;
@@ -116,9 +117,10 @@ __device__ __noinline__ void run_pass(const Unit& u, const JobsArgs& a, float2* 
     else pass_rows<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
 }
 
-__device__ __noinline__ void run_split_merge(const Unit& u, const JobsArgs& a)
+__device__ __noinline__ void run_split_merge(const UnitRec& r, const JobsArgs& a)
 {
-    const LargeDesc d = a.large[u.job];
+    const Unit& u = r.u;
+    const LargeDesc d = r.big;
     const long long M = 1ll << u.log2a;
     const float2* twn = a.tw + 2 * M;
     const float2* src = pick(d, u.sel & 15);
@@ -133,59 +135,61 @@ __device__ __noinline__ void run_split_merge(const Unit& u, const JobsArgs& a)
 
 #define CKG_SINGLE_CASES(OP)                                                          \
     switch (u.log2a) {                                                                \
-    case 0: if constexpr (OP <= U_C2C_INV) run_single<OP, 0>(u, a, smem); break;      \
-    case 1: if constexpr (OP <= U_C2C_INV) run_single<OP, 1>(u, a, smem); break;      \
-    case 2: run_single<OP, 2>(u, a, smem); break;                                     \
-    case 3: run_single<OP, 3>(u, a, smem); break;                                     \
-    case 4: run_single<OP, 4>(u, a, smem); break;                                     \
-    case 5: run_single<OP, 5>(u, a, smem); break;                                     \
-    case 6: run_single<OP, 6>(u, a, smem); break;                                     \
-    case 7: run_single<OP, 7>(u, a, smem); break;                                     \
-    case 8: run_single<OP, 8>(u, a, smem); break;                                     \
-    case 9: run_single<OP, 9>(u, a, smem); break;                                     \
-    case 10: run_single<OP, 10>(u, a, smem); break;                                   \
-    case 11: run_single<OP, 11>(u, a, smem); break;                                   \
-    case 12: run_single<OP, 12>(u, a, smem); break;                                   \
+    case 0: if constexpr (OP <= U_C2C_INV) run_single<OP, 0>(r, a, smem); break;      \
+    case 1: if constexpr (OP <= U_C2C_INV) run_single<OP, 1>(r, a, smem); break;      \
+    case 2: run_single<OP, 2>(r, a, smem); break;                                     \
+    case 3: run_single<OP, 3>(r, a, smem); break;                                     \
+    case 4: run_single<OP, 4>(r, a, smem); break;                                     \
+    case 5: run_single<OP, 5>(r, a, smem); break;                                     \
+    case 6: run_single<OP, 6>(r, a, smem); break;                                     \
+    case 7: run_single<OP, 7>(r, a, smem); break;                                     \
+    case 8: run_single<OP, 8>(r, a, smem); break;                                     \
+    case 9: run_single<OP, 9>(r, a, smem); break;                                     \
+    case 10: run_single<OP, 10>(r, a, smem); break;                                   \
+    case 11: run_single<OP, 11>(r, a, smem); break;                                   \
+    case 12: run_single<OP, 12>(r, a, smem); break;                                   \
     default: break;                                                                   \
     }
 
 #define CKG_PASS_CASES(OP)                                                            \
     switch (u.log2a) {                                                                \
-    case 6: run_pass<OP, 6>(u, a, smem); break;                                       \
-    case 7: run_pass<OP, 7>(u, a, smem); break;                                       \
-    case 8: run_pass<OP, 8>(u, a, smem); break;                                       \
-    case 9: run_pass<OP, 9>(u, a, smem); break;                                       \
-    case 10: run_pass<OP, 10>(u, a, smem); break;                                     \
+    case 6: run_pass<OP, 6>(r, a, smem); break;                                       \
+    case 7: run_pass<OP, 7>(r, a, smem); break;                                       \
+    case 8: run_pass<OP, 8>(r, a, smem); break;                                       \
+    case 9: run_pass<OP, 9>(r, a, smem); break;                                       \
+    case 10: run_pass<OP, 10>(r, a, smem); break;                                     \
     default: break;                                                                   \
     }
 
 template <int OP>
-__device__ __forceinline__ void single_switch(const Unit& u, const JobsArgs& a, float2* smem)
+__device__ __forceinline__ void single_switch(const UnitRec& r, const JobsArgs& a, float2* smem)
 {
+    const Unit& u = r.u;
     CKG_SINGLE_CASES(OP)
 }
 
 template <int OP>
-__device__ __forceinline__ void pass_switch(const Unit& u, const JobsArgs& a, float2* smem)
+__device__ __forceinline__ void pass_switch(const UnitRec& r, const JobsArgs& a, float2* smem)
 {
+    const Unit& u = r.u;
     CKG_PASS_CASES(OP)
 }
 
-__device__ __forceinline__ void dispatch(const Unit& u, const JobsArgs& a, float2* smem)
+__device__ __forceinline__ void dispatch(const UnitRec& r, const JobsArgs& a, float2* smem)
 {
-    switch (u.op) {
-    case U_C2C_FWD: single_switch<U_C2C_FWD>(u, a, smem); break;
-    case U_C2C_INV: single_switch<U_C2C_INV>(u, a, smem); break;
-    case U_R2C: single_switch<U_R2C>(u, a, smem); break;
-    case U_C2R: single_switch<U_C2R>(u, a, smem); break;
-    case U_RTINY_FWD: run_rtiny(u, a, false); break;
-    case U_RTINY_INV: run_rtiny(u, a, true); break;
-    case U_COLS_FWD: pass_switch<U_COLS_FWD>(u, a, smem); break;
-    case U_COLS_INV: pass_switch<U_COLS_INV>(u, a, smem); break;
-    case U_ROWS_FWD: pass_switch<U_ROWS_FWD>(u, a, smem); break;
-    case U_ROWS_INV: pass_switch<U_ROWS_INV>(u, a, smem); break;
+    switch (r.u.op) {
+    case U_C2C_FWD: single_switch<U_C2C_FWD>(r, a, smem); break;
+    case U_C2C_INV: single_switch<U_C2C_INV>(r, a, smem); break;
+    case U_R2C: single_switch<U_R2C>(r, a, smem); break;
+    case U_C2R: single_switch<U_C2R>(r, a, smem); break;
+    case U_RTINY_FWD: run_rtiny(r, false); break;
+    case U_RTINY_INV: run_rtiny(r, true); break;
+    case U_COLS_FWD: pass_switch<U_COLS_FWD>(r, a, smem); break;
+    case U_COLS_INV: pass_switch<U_COLS_INV>(r, a, smem); break;
+    case U_ROWS_FWD: pass_switch<U_ROWS_FWD>(r, a, smem); break;
+    case U_ROWS_INV: pass_switch<U_ROWS_INV>(r, a, smem); break;
     case U_SPLIT:
-    case U_MERGE: run_split_merge(u, a); break;
+    case U_MERGE: run_split_merge(r, a); break;
     default: break;
     }
 }
@@ -193,32 +197,72 @@ __device__ __forceinline__ void dispatch(const Unit& u, const JobsArgs& a, float
 __global__ void __launch_bounds__(kJobThreads, kJobCtasPerSm) k_jobs(JobsArgs a)
 {
     extern __shared__ __align__(128) float2 smem[];
-    __shared__ int s_unit;
+    __shared__ __align__(128) UnitRec s_rec[2];
+    __shared__ __align__(8) unsigned long long s_bar[2];
+    __shared__ int s_idx[2];
     __shared__ int s_ok;
-    // The next unit is claimed when the current one starts, so the atomic's
-    // round trip overlaps the work.  Still deadlock-free: the lowest-indexed
-    // unit in progress depends only on lower indices, all of which are done.
-    if (threadIdx.x == 0) s_unit = atomicAdd(a.head, 1);
-    for (;;) {
-        __syncthreads();
-        const int ui = s_unit;
-        if (ui >= a.nunits) break;
-        const Unit u = a.units[ui];
-        int next = 0;
-        if (threadIdx.x == 0) {
-            next = atomicAdd(a.head, 1);
-            s_ok = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err) : 1;
+    // Iteration `it` works on the unit in slot it & 1 (index s_idx, record
+    // s_rec).  Thread 0 keeps two units ahead: while the CTA works on one
+    // unit, the next unit's record is on its way into the other slot (one
+    // bulk copy) and the claim after it (one atomic add) is in flight.
+    // Still deadlock-free: a CTA claims in increasing order, so the
+    // lowest-indexed unfinished unit is some CTA's current unit, and it
+    // depends only on lower indices, all of which are finished.
+    constexpr uint32_t kRecBytes = sizeof(UnitRec);
+    int next = 0;                         // thread 0: the claim after the slot being filled
+    if (threadIdx.x == 0) {
+        mbar_init(smem_addr(&s_bar[0]), 1);
+        mbar_init(smem_addr(&s_bar[1]), 1);
+        fence_mbar_init();
+        const int cur = atomicAdd(a.head, 1);
+        if (cur < a.nunits) {
+            mbar_arrive_expect_tx(smem_addr(&s_bar[0]), kRecBytes);
+            bulk_load(smem_addr(&s_rec[0]), a.recs + cur, kRecBytes, smem_addr(&s_bar[0]));
         }
-        __syncthreads();
-        if (s_ok) dispatch(u, a, smem);
-        __syncthreads();
+        s_idx[0] = cur;
+        next = atomicAdd(a.head, 1);
+    }
+    __syncthreads();
+    int stuck = -1;                       // thread 0: slot whose copy never completed
+#pragma unroll 1
+    for (int it = 0;; ++it) {
+        const int slot = it & 1;
+        if (s_idx[slot] >= a.nunits) break;
         if (threadIdx.x == 0) {
-            if (u.job >= 0) {
-                __threadfence();
-                atomicAdd(a.done + u.job, 1);
+            const bool got = mbar_wait(smem_addr(&s_bar[slot]), (uint32_t)(it >> 1) & 1u, a.err);
+            if (got && next < a.nunits) {
+                // the other slot was last read before the barrier that ended
+                // the previous iteration
+                fence_proxy_async_shared();
+                mbar_arrive_expect_tx(smem_addr(&s_bar[slot ^ 1]), kRecBytes);
+                bulk_load(smem_addr(&s_rec[slot ^ 1]), a.recs + next, kRecBytes, smem_addr(&s_bar[slot ^ 1]));
+                s_idx[slot ^ 1] = next;
+                next = atomicAdd(a.head, 1);
+            } else {
+                s_idx[slot ^ 1] = a.nunits;      // no unit left: the loop ends after this one
             }
-            s_unit = next;
+            if (!got) {
+                stuck = slot;
+                s_ok = -1;
+            } else {
+                const Unit& u = s_rec[slot].u;
+                s_ok = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err) : 1;
+            }
         }
+        __syncthreads();
+        const int ok = s_ok;
+        if (ok < 0) break;                   // a record never arrived (error word set)
+        if (ok) dispatch(s_rec[slot], a, smem);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_rec[slot].u.job >= 0) {
+            __threadfence();
+            atomicAdd(a.done + s_rec[slot].u.job, 1);
+        }
+    }
+    // after a timed-out copy, wait for it again (bounded) before the CTA's
+    // shared memory goes away; on the normal path no copy is in flight
+    if (threadIdx.x == 0 && stuck >= 0) {
+        for (int k = 0; k < 2; ++k) mbar_wait(smem_addr(&s_bar[stuck]), (uint32_t)k, nullptr);
     }
 }
 

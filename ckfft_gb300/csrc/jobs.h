@@ -2,8 +2,8 @@
 //
 // A run of mixed transforms is flattened into a queue of units that the
 // persistent CTAs pop with one atomic add each:
-//   * single-CTA units: up to 512/T frames of one kind and size, each frame
-//     with its own input / output pointer (FrameDesc);
+//   * single-CTA units: up to min(256/T, 64) frames of one kind and size,
+//     each frame with its own input / output pointer (FrameDesc);
 //   * phase units of a multi-pass transform (LargeDesc): a merge range, a set
 //     of column tiles, a set of row tiles, or a split range.  A phase unit
 //     names how many units of its transform must have finished first; every
@@ -40,9 +40,9 @@ struct Unit {
     int op;
     int log2a;
     int log2b;
-    int job;       // LargeDesc index, -1 for single-CTA units
+    int job;       // multi-pass transform index (its counter), -1 for single-CTA units
     int need;      // units of `job` that must have finished before this one
-    int first;     // first frame (single), first tile (pass), first element (split / merge)
+    int first;     // first tile (pass), first element (split / merge)
     int count;     // frames, tiles or elements
     int sel;       // source selector | destination selector << 4 (phase units)
 };
@@ -59,12 +59,23 @@ struct LargeDesc {
     long long pad;
 };
 
+// Frame pointers one single-CTA unit carries at most.
+constexpr int kRecFrames = 64;
+
+// Everything one unit needs, in one fixed-size record: a CTA copies the next
+// unit's record into shared memory (one bulk copy) while it works on the
+// current one, so a unit starts without a chain of dependent global loads.
+struct UnitRec {
+    Unit u;
+    LargeDesc big;                  // phase units: the transform's buffers
+    FrameDesc frames[kRecFrames];   // single-CTA units: u.count frames
+};
+static_assert(sizeof(UnitRec) % 16 == 0, "records are bulk-copied in 16-byte units");
+
 struct JobsArgs {
-    const Unit* units;
+    const UnitRec* recs;
     int nunits;
-    const FrameDesc* frames;
-    const LargeDesc* large;
-    int* done;         // one counter per LargeDesc
+    int* done;         // one counter per multi-pass transform
     int* head;         // queue head
     const float2* tw;
     unsigned* err;

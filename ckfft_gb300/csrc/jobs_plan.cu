@@ -223,7 +223,9 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
     std::stable_sort(order.begin(), order.end(), [](const auto& x, const auto& y) { return x.first.second > y.first.second; });
     for (auto& kv : order) {
         const int op = kv.first.first, l2 = kv.first.second;
-        const int per = (op == U_RTINY_FWD || op == U_RTINY_INV) ? kJobThreads : kJobThreads / single_threads(l2);
+        const int per = std::min((op == U_RTINY_FWD || op == U_RTINY_INV) ? kJobThreads
+                                                                           : kJobThreads / single_threads(l2),
+                                 kRecFrames);
         const std::vector<FrameDesc>& fr = kv.second;
         for (size_t i = 0; i < fr.size(); i += per) {
             const int cnt = (int)std::min<size_t>(per, fr.size() - i);
@@ -301,6 +303,24 @@ long long job_algo_bytes(const CkFftCudaJob& j)
     return (long long)j.count * (real ? 4ll * j.n + 8ll * (j.n / 2 + 1) : 16ll * j.n);
 }
 
+// The queue as fixed-size records: each unit with its transform's buffers
+// (phase units) or its frame pointers (single-CTA units) inline.
+static void make_records(const Built& b, float2* scratch, std::vector<UnitRec>* recs)
+{
+    recs->assign(b.units.size(), UnitRec{});
+    for (size_t i = 0; i < b.units.size(); ++i) {
+        UnitRec& r = (*recs)[i];
+        r.u = b.units[i];
+        if (r.u.job >= 0) {
+            r.big = b.large[r.u.job];
+            r.big.scratch = scratch + b.scratch_off[r.u.job];
+        } else {
+            for (int f = 0; f < r.u.count; ++f) r.frames[f] = b.frames[r.u.first + f];
+            r.u.first = 0;
+        }
+    }
+}
+
 void free_run_slot(RunSlot* r)
 {
     cudaFree(r->dev);
@@ -328,11 +348,7 @@ int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunS
     if (!build_units(cv, jobs, njobs, &b)) return 0;
     if (b.units.empty()) return 1;
     size_t off = 0;
-    const size_t o_units = off; off += sizeof(Unit) * b.units.size();
-    off = (off + 15) / 16 * 16;
-    const size_t o_frames = off; off += sizeof(FrameDesc) * b.frames.size();
-    off = (off + 15) / 16 * 16;
-    const size_t o_large = off; off += sizeof(LargeDesc) * b.large.size();
+    const size_t o_recs = off; off += sizeof(UnitRec) * b.units.size();
     off = (off + 15) / 16 * 16;
     const size_t o_done = off; off += sizeof(int) * (b.large.size() + 1);
     const size_t total = off + 16;
@@ -352,20 +368,14 @@ int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunS
         set_last_error(cudaGetErrorString(e));
         return -1;
     }
-    memcpy(r->host + o_units, b.units.data(), sizeof(Unit) * b.units.size());
-    memcpy(r->host + o_frames, b.frames.data(), sizeof(FrameDesc) * b.frames.size());
-    LargeDesc* ld = (LargeDesc*)(r->host + o_large);
-    for (size_t i = 0; i < b.large.size(); ++i) {
-        ld[i] = b.large[i];
-        ld[i].scratch = scratch + b.scratch_off[i];
-    }
+    std::vector<UnitRec> recs;
+    make_records(b, scratch, &recs);
+    memcpy(r->host + o_recs, recs.data(), sizeof(UnitRec) * recs.size());
     memset(r->host + o_done, 0, sizeof(int) * (b.large.size() + 1));
     char* base = (char*)r->dev;
     JobsArgs a{};
-    a.units = (const Unit*)(base + o_units);
+    a.recs = (const UnitRec*)(base + o_recs);
     a.nunits = (int)b.units.size();
-    a.frames = (const FrameDesc*)(base + o_frames);
-    a.large = (const LargeDesc*)(base + o_large);
     a.done = (int*)(base + o_done);
     a.head = a.done + b.large.size();
     a.tw = cv.tw;
@@ -410,11 +420,7 @@ cudaError_t upload(const Built& b, ContextView cv, void** dmem, float2** scratch
                    cudaStream_t s, bool async_alloc)
 {
     size_t off = 0;
-    const size_t o_units = off; off += sizeof(Unit) * b.units.size();
-    off = (off + 15) / 16 * 16;
-    const size_t o_frames = off; off += sizeof(FrameDesc) * b.frames.size();
-    off = (off + 15) / 16 * 16;
-    const size_t o_large = off; off += sizeof(LargeDesc) * b.large.size();
+    const size_t o_recs = off; off += sizeof(UnitRec) * b.units.size();
     off = (off + 15) / 16 * 16;
     const size_t o_done = off; off += sizeof(int) * (b.large.size() + 1);   // + queue head
     const size_t total = off + 16;
@@ -427,19 +433,15 @@ cudaError_t upload(const Built& b, ContextView cv, void** dmem, float2** scratch
         if (e != cudaSuccess) return e;
     }
     std::vector<char> host(total, 0);
-    memcpy(host.data() + o_units, b.units.data(), sizeof(Unit) * b.units.size());
-    memcpy(host.data() + o_frames, b.frames.data(), sizeof(FrameDesc) * b.frames.size());
-    std::vector<LargeDesc> large = b.large;
-    for (size_t i = 0; i < large.size(); ++i) large[i].scratch = *scratch + b.scratch_off[i];
-    memcpy(host.data() + o_large, large.data(), sizeof(LargeDesc) * large.size());
+    std::vector<UnitRec> recs;
+    make_records(b, *scratch, &recs);
+    memcpy(host.data() + o_recs, recs.data(), sizeof(UnitRec) * recs.size());
     // pageable source: the call returns once the data is staged, so `host` may go
     e = cudaMemcpyAsync(*dmem, host.data(), total, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return e;
     char* base = (char*)*dmem;
-    a->units = (const Unit*)(base + o_units);
+    a->recs = (const UnitRec*)(base + o_recs);
     a->nunits = (int)b.units.size();
-    a->frames = (const FrameDesc*)(base + o_frames);
-    a->large = (const LargeDesc*)(base + o_large);
     a->done = (int*)(base + o_done);
     a->head = a->done + b.large.size();
     a->tw = cv.tw;
