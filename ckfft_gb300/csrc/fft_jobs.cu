@@ -38,25 +38,19 @@ __device__ __forceinline__ bool wait_counter(const int* p, int need, unsigned* e
 
 // ----------------------------------------------------------- unit bodies
 
-// The unit's frames, kJobThreads / T at a time (one per group of T threads).
 template <int OP, int L>
 __device__ __noinline__ void run_single(const UnitRec& r, const JobsArgs& a, float2* smem)
 {
     using C = SmallCfg<L>;
-    constexpr int G = kJobThreads / C::T;
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const bool live = g < r.u.count;
+    FrameDesc fd{nullptr, nullptr};
+    if (live) fd = r.frames[g];
     const PaddedView view{smem + g * C::SLOT};
-#pragma unroll 1
-    for (int k = 0; k < r.u.count; k += G) {
-        const bool live = k + g < r.u.count;
-        FrameDesc fd{nullptr, nullptr};
-        if (live) fd = r.frames[k + g];
-        if constexpr (OP == U_C2C_FWD) frame_c2c<L, false>(fd.in, fd.out, live, t, view, a.tw);
-        else if constexpr (OP == U_C2C_INV) frame_c2c<L, true>(fd.in, fd.out, live, t, view, a.tw);
-        else if constexpr (OP == U_R2C) frame_r2c<L>(fd.in, fd.out, live, t, view, a.tw);
-        else frame_c2r<L>(fd.in, fd.out, live, t, view, a.tw);
-        xsync<C::WARP>();
-    }
+    if constexpr (OP == U_C2C_FWD) frame_c2c<L, false>(fd.in, fd.out, live, t, view, a.tw);
+    else if constexpr (OP == U_C2C_INV) frame_c2c<L, true>(fd.in, fd.out, live, t, view, a.tw);
+    else if constexpr (OP == U_R2C) frame_r2c<L>(fd.in, fd.out, live, t, view, a.tw);
+    else frame_c2r<L>(fd.in, fd.out, live, t, view, a.tw);
 }
 
 // Real n = 1, 2, 4 closed forms (src/ckfft/fft_real.cpp:20-93), one frame per thread.
@@ -116,18 +110,11 @@ __device__ __noinline__ void run_pass(const UnitRec& r, const JobsArgs& a, float
     const float2* src = pick(d, u.sel & 15);
     float2* dst = pick(d, u.sel >> 4);
     float2* my = smem + s * P::SLOTS;
-    constexpr int S = kJobThreads / P::THREADS;
-    // u.count tiles from u.first, S at a time (one per subgroup)
-#pragma unroll 1
-    for (int k = 0; k < u.count; k += S) {
-        const bool live = k + s < u.count;
-        const long long tile = (long long)u.first + (live ? k + s : 0);
-        if constexpr (OP == U_COLS_FWD) pass_cols<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw, live);
-        else if constexpr (OP == U_COLS_INV) pass_cols<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw, live);
-        else if constexpr (OP == U_ROWS_FWD) pass_rows<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw, live);
-        else pass_rows<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw, live);
-        __syncthreads();
-    }
+    const long long tile = (long long)u.first + s;
+    if constexpr (OP == U_COLS_FWD) pass_cols<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_COLS_INV) pass_cols<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_ROWS_FWD) pass_rows<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else pass_rows<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
 }
 
 __device__ __noinline__ void run_split_merge(const UnitRec& r, const JobsArgs& a)

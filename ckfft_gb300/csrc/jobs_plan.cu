@@ -61,12 +61,6 @@ static int single_threads(int l)
 }
 
 constexpr int kElemsPerUnit = kJobThreads * 16;  // split / merge work per unit
-// Rounds of work per unit (frame groups of a single-CTA unit, tiles per
-// subgroup of a pass unit).  Two rounds measured slower on GB300 (workload
-// 4: 1958 vs 2156 GB/s; 2^16 phase units 1950 vs 2374): fewer units leave
-// the phases of a transform less to overlap with.
-constexpr int kSingleRounds = 1;
-constexpr int kPassRounds = 1;
 
 struct Built {
     std::vector<Unit> units;
@@ -189,13 +183,12 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
                 b->scratch_elems += 1ll << lc;
                 const int la = lc / 2, lb = lc - la;
                 const PassShape pa = pass_shape(la), pb = pass_shape(lb);
-                // pass units of kPassRounds tiles per subgroup
-                const int sa = kPassRounds * (kJobThreads / pa.threads), sb = kPassRounds * (kJobThreads / pb.threads);
+                const int sa = kJobThreads / pa.threads, sb = kJobThreads / pb.threads;
                 const int tiles_a = (1 << lb) / pa.cols, tiles_b = (1 << la) / pb.cols;
                 int done = 0, p = 0, added = 0;   // units of earlier phases, of this phase
                 auto add_pass = [&](int op, int ls, int other, int tiles, int per, int src, int dst) {
                     for (int t = 0; t < tiles; t += per, ++added)
-                        phase[p].push_back({op, ls, other, job, done, t, std::min(per, tiles - t), src | (dst << 4)});
+                        phase[p].push_back({op, ls, other, job, done, t, per, src | (dst << 4)});
                 };
                 auto add_elems = [&](int op, long long count, int src, int dst) {
                     for (long long e = 0; e < count; e += kElemsPerUnit, ++added)
@@ -231,7 +224,7 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
     for (auto& kv : order) {
         const int op = kv.first.first, l2 = kv.first.second;
         const int per = std::min((op == U_RTINY_FWD || op == U_RTINY_INV) ? kJobThreads
-                                                                           : kSingleRounds * (kJobThreads / single_threads(l2)),
+                                                                           : kJobThreads / single_threads(l2),
                                  kRecFrames);
         const std::vector<FrameDesc>& fr = kv.second;
         for (size_t i = 0; i < fr.size(); i += per) {
