@@ -197,22 +197,27 @@ __device__ __forceinline__ void dispatch(const UnitRec& r, const JobsArgs& a, fl
 __global__ void __launch_bounds__(kJobThreads, kJobCtasPerSm) k_jobs(JobsArgs a)
 {
     extern __shared__ __align__(128) float2 smem[];
-    __shared__ __align__(128) UnitRec s_rec[2];
-    __shared__ __align__(8) unsigned long long s_bar[2];
-    __shared__ int s_idx[2];
-    __shared__ int s_ok;
-    // Iteration `it` works on the unit in slot it & 1 (index s_idx, record
-    // s_rec).  Thread 0 keeps two units ahead: while the CTA works on one
-    // unit, the next unit's record is on its way into the other slot (one
-    // bulk copy) and the claim after it (one atomic add) is in flight.
-    // Still deadlock-free: a CTA claims in increasing order, so the
-    // lowest-indexed unfinished unit is some CTA's current unit, and it
-    // depends only on lower indices, all of which are finished.
+    constexpr int kSlots = 3;
+    __shared__ __align__(128) UnitRec s_rec[kSlots];
+    __shared__ __align__(8) unsigned long long s_bar[kSlots];
+    __shared__ int s_idx[kSlots];
+    __shared__ int s_ok[kSlots];
+    // Iteration `it` works on the unit in slot it % 3 (index, record, go /
+    // no-go).  Thread 0 keeps two units ahead: while the CTA works on one
+    // unit, the next unit's record is on its way into the following slot
+    // (one bulk copy) and the claim after it (one atomic add) is in flight.
+    // One CTA barrier per unit: with three slots, the slot being refilled was
+    // last read two units ago, before the previous unit's barrier; a phase
+    // unit's completion is counted per warp (every warp fences and adds one),
+    // so no barrier waits for the slowest warp at the end of a unit.
+    // Deadlock-free: a CTA claims in increasing order, so the lowest-indexed
+    // unfinished unit is some CTA's current unit, and it depends only on lower
+    // indices, all of which are finished.
     constexpr uint32_t kRecBytes = sizeof(UnitRec);
     int next = 0;                         // thread 0: the claim after the slot being filled
+    int stuck = -1;                       // thread 0: slot whose copy never completed
     if (threadIdx.x == 0) {
-        mbar_init(smem_addr(&s_bar[0]), 1);
-        mbar_init(smem_addr(&s_bar[1]), 1);
+        for (int k = 0; k < kSlots; ++k) mbar_init(smem_addr(&s_bar[k]), 1);
         fence_mbar_init();
         const int cur = atomicAdd(a.head, 1);
         if (cur < a.nunits) {
@@ -223,40 +228,40 @@ __global__ void __launch_bounds__(kJobThreads, kJobCtasPerSm) k_jobs(JobsArgs a)
         next = atomicAdd(a.head, 1);
     }
     __syncthreads();
-    int stuck = -1;                       // thread 0: slot whose copy never completed
 #pragma unroll 1
-    for (int it = 0;; ++it) {
-        const int slot = it & 1;
+    for (int it = 0, slot = 0;; ++it, slot = slot == kSlots - 1 ? 0 : slot + 1) {
         if (s_idx[slot] >= a.nunits) break;
+        const int nslot = slot == kSlots - 1 ? 0 : slot + 1;
         if (threadIdx.x == 0) {
-            const bool got = mbar_wait(smem_addr(&s_bar[slot]), (uint32_t)(it >> 1) & 1u, a.err);
+            const bool got = mbar_wait(smem_addr(&s_bar[slot]), (uint32_t)(it / kSlots) & 1u, a.err);
             if (got && next < a.nunits) {
-                // the other slot was last read before the barrier that ended
-                // the previous iteration
                 fence_proxy_async_shared();
-                mbar_arrive_expect_tx(smem_addr(&s_bar[slot ^ 1]), kRecBytes);
-                bulk_load(smem_addr(&s_rec[slot ^ 1]), a.recs + next, kRecBytes, smem_addr(&s_bar[slot ^ 1]));
-                s_idx[slot ^ 1] = next;
+                mbar_arrive_expect_tx(smem_addr(&s_bar[nslot]), kRecBytes);
+                bulk_load(smem_addr(&s_rec[nslot]), a.recs + next, kRecBytes, smem_addr(&s_bar[nslot]));
+                s_idx[nslot] = next;
                 next = atomicAdd(a.head, 1);
             } else {
-                s_idx[slot ^ 1] = a.nunits;      // no unit left: the loop ends after this one
+                s_idx[nslot] = a.nunits;         // no unit left: the loop ends after this one
             }
             if (!got) {
                 stuck = slot;
-                s_ok = -1;
+                s_ok[slot] = -1;
             } else {
                 const Unit& u = s_rec[slot].u;
-                s_ok = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err) : 1;
+                s_ok[slot] = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err) : 1;
             }
         }
         __syncthreads();
-        const int ok = s_ok;
+        const int ok = s_ok[slot];
         if (ok < 0) break;                   // a record never arrived (error word set)
         if (ok) dispatch(s_rec[slot], a, smem);
-        __syncthreads();
-        if (threadIdx.x == 0 && s_rec[slot].u.job >= 0) {
-            __threadfence();
-            atomicAdd(a.done + s_rec[slot].u.job, 1);
+        const int job = s_rec[slot].u.job;
+        if (job >= 0) {
+            __syncwarp();
+            if ((threadIdx.x & 31) == 0) {
+                __threadfence();
+                atomicAdd(a.done + job, 1);
+            }
         }
     }
     // after a timed-out copy, wait for it again (bounded) before the CTA's

@@ -314,6 +314,7 @@ static void make_records(const Built& b, float2* scratch, std::vector<UnitRec>* 
         if (r.u.job >= 0) {
             r.big = b.large[r.u.job];
             r.big.scratch = scratch + b.scratch_off[r.u.job];
+            r.u.need *= kJobThreads / 32;      // completion is counted per warp
         } else {
             for (int f = 0; f < r.u.count; ++f) r.frames[f] = b.frames[r.u.first + f];
             r.u.first = 0;
