@@ -84,6 +84,9 @@ def _declare_extras(lib):
         if hasattr(lib, f):
             getattr(lib, f).restype = i
             getattr(lib, f).argtypes = [vp, i, ll, vp, ll, ll, vp, ll, ll, vp]
+    if hasattr(lib, "CkFftCudaSelfTestWait"):
+        lib.CkFftCudaSelfTestWait.restype = i
+        lib.CkFftCudaSelfTestWait.argtypes = [vp, i]
     if hasattr(lib, "CkFftCudaStft"):
         lib.CkFftCudaStft.restype = i
         lib.CkFftCudaStft.argtypes = [vp, i, ll, vp, ll, ll, vp, C.c_float, vp, vp]

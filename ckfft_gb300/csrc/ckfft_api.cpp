@@ -178,7 +178,7 @@ cudaError_t grow(void** p, size_t* cap, size_t need)
     cudaFree(*p);
     *p = nullptr;
     *cap = 0;
-    cudaError_t e = cudaMalloc(p, need);
+    cudaError_t e = ckg::dev_malloc(p, need);
     if (e == cudaSuccess) *cap = need;
     return e;
 }
@@ -847,7 +847,7 @@ CkFftContext* CkFftInit(int nMax, CkFftDirection direction, void* buf, size_t* b
     if (e != cudaSuccess) { cuda_fail("no CUDA device", e); goto fail_out; }
     if ((e = ckg::prepare_device()) != cudaSuccess) { cuda_fail("kernel set-up", e); goto fail_out; }
     ckg::build_twiddles(c->log2max, tab);
-    if ((e = cudaMalloc(&c->dtw, sizeof(float2) * tab.size())) != cudaSuccess) { cuda_fail("cudaMalloc(twiddles)", e); goto fail_out; }
+    if ((e = ckg::dev_malloc((void**)&c->dtw, sizeof(float2) * tab.size())) != cudaSuccess) { cuda_fail("cudaMalloc(twiddles)", e); goto fail_out; }
     if ((e = cudaMemcpy(c->dtw, tab.data(), sizeof(float2) * tab.size(), cudaMemcpyHostToDevice)) != cudaSuccess) { cuda_fail("cudaMemcpy(twiddles)", e); goto fail_out; }
     c->pool = new (std::nothrow) LanePool();
     if (!c->pool) { set_error("out of host memory"); goto fail_out; }

@@ -118,8 +118,36 @@ static cudaError_t prepare_pool(int dev)
     return cudaSuccess;
 }
 
+// CKFFT_CUDA_FAIL_ALLOC=k: the k-th device allocation the library requests
+// (counting from 1 over every allocation site) fails with
+// cudaErrorMemoryAllocation -- one injected failure per process, for tests of
+// the failure paths.  Unset or 0: off.
+bool injected_alloc_failure()
+{
+    static const long long target = [] {
+        const char* v = std::getenv("CKFFT_CUDA_FAIL_ALLOC");
+        return v ? std::atoll(v) : 0ll;
+    }();
+    if (target <= 0) return false;
+    static std::atomic<long long> seen{0};
+    return seen.fetch_add(1, std::memory_order_relaxed) + 1 == target;
+}
+
+cudaError_t dev_malloc(void** p, size_t bytes)
+{
+    if (injected_alloc_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
 cudaError_t pool_alloc_async(void** p, size_t bytes, cudaStream_t s)
 {
+    if (injected_alloc_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;

@@ -23,10 +23,11 @@ namespace ckg {
 
 constexpr unsigned kErrCounterTimeout = 2u;
 
-__device__ __forceinline__ bool wait_counter(const int* p, int need, unsigned* err)
+__device__ __forceinline__ bool wait_counter(const int* p, int need, unsigned* err, int tries)
 {
+    if (tries <= 0) tries = 1 << 26;
 #pragma unroll 1
-    for (int it = 0; it < (1 << 26); ++it) {
+    for (int it = 0; it < tries; ++it) {
         int v;
         asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
         if (v >= need) return true;
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(kJobThreads, kJobCtasPerSm) k_jobs(JobsArgs a)
                 s_ok[slot] = -1;
             } else {
                 const Unit& u = s_rec[slot].u;
-                s_ok[slot] = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err) : 1;
+                s_ok[slot] = (u.job >= 0 && u.need > 0) ? (int)wait_counter(a.done + u.job, u.need, a.err, a.wait_tries) : 1;
             }
         }
         __syncthreads();
@@ -325,6 +326,12 @@ int jobs_grid()
     const int g = per * (sms > 0 ? sms : 1);
     if (dev >= 0 && dev < 64) cache[dev] = g;
     return g;
+}
+
+cudaError_t launch_jobs_one(const JobsArgs& a, cudaStream_t s)
+{
+    k_jobs<<<1, kJobThreads, jobs_smem_bytes(), s>>>(a);
+    return cudaGetLastError();
 }
 
 // Enqueues the job kernel (the caller counts the launch).

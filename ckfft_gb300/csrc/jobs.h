@@ -79,6 +79,7 @@ struct JobsArgs {
     int* head;         // queue head
     const float2* tw;
     unsigned* err;
+    int wait_tries;    // bound of a phase unit's counter wait; 0: the default (seconds)
 };
 
 // 256 threads per CTA and 64 registers: four CTAs -- four independent unit
@@ -118,6 +119,8 @@ long long job_algo_bytes(const CkFftCudaJob& j);
 
 // Launches the job kernel on all resident CTAs of the current device.
 cudaError_t launch_jobs(const JobsArgs& a, cudaStream_t s);
+// The job kernel on one CTA (self-test of the bounded waits).
+cudaError_t launch_jobs_one(const JobsArgs& a, cudaStream_t s);
 // Shared memory the job kernel needs (bytes) and resident CTAs per SM.
 size_t jobs_smem_bytes();
 int jobs_grid();

@@ -337,7 +337,7 @@ static cudaError_t grow_dev(void** p, size_t* cap, size_t need)
     *p = nullptr;
     *cap = 0;
     const size_t want = need + need / 4;
-    cudaError_t e = cudaMalloc(p, want);
+    cudaError_t e = dev_malloc(p, want);
     if (e == cudaSuccess) *cap = want;
     return e;
 }
@@ -425,12 +425,12 @@ cudaError_t upload(const Built& b, ContextView cv, void** dmem, float2** scratch
     off = (off + 15) / 16 * 16;
     const size_t o_done = off; off += sizeof(int) * (b.large.size() + 1);   // + queue head
     const size_t total = off + 16;
-    cudaError_t e = async_alloc ? pool_alloc_async(dmem, total, s) : cudaMalloc(dmem, total);
+    cudaError_t e = async_alloc ? pool_alloc_async(dmem, total, s) : dev_malloc(dmem, total);
     if (e != cudaSuccess) return e;
     *scratch = nullptr;
     if (b.scratch_elems) {
         e = async_alloc ? pool_alloc_async((void**)scratch, sizeof(float2) * b.scratch_elems, s)
-                        : cudaMalloc((void**)scratch, sizeof(float2) * b.scratch_elems);
+                        : dev_malloc((void**)scratch, sizeof(float2) * b.scratch_elems);
         if (e != cudaSuccess) return e;
     }
     std::vector<char> host(total, 0);

@@ -158,5 +158,8 @@ unsigned take_device_error();
 // device; the pool keeps freed memory (release threshold: unlimited), so
 // repeated calls do not map and unmap device memory.  Free with cudaFreeAsync.
 cudaError_t pool_alloc_async(void** p, size_t bytes, cudaStream_t s);
+// cudaMalloc through the library's fault-injection point
+// (CKFFT_CUDA_FAIL_ALLOC=k fails the k-th allocation of the process).
+cudaError_t dev_malloc(void** p, size_t bytes);
 
 }  // namespace ckg

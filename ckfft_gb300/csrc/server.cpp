@@ -379,12 +379,12 @@ CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_bud
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
         // resident buffers: scratch arena, and descriptor space for large runs
         if (e == cudaSuccess && s->arena) {
-            e = cudaMalloc((void**)&sl.run.scratch, s->arena);
+            e = ckg::dev_malloc((void**)&sl.run.scratch, s->arena);
             if (e == cudaSuccess) sl.run.scratch_cap = s->arena;
         }
         if (e == cudaSuccess) {
             const size_t desc = 8u << 20;
-            e = cudaMalloc(&sl.run.dev, desc);
+            e = ckg::dev_malloc(&sl.run.dev, desc);
             if (e == cudaSuccess) sl.run.dev_cap = desc;
             if (e == cudaSuccess) e = cudaHostAlloc((void**)&sl.run.host, desc, cudaHostAllocDefault);
             if (e == cudaSuccess) sl.run.host_cap = desc;

@@ -60,10 +60,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase)
 }
 
 // Waits for `phase` of the barrier; false (and the error word set) on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, unsigned* err)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, unsigned* err, int tries = kWaitTries)
 {
 #pragma unroll 1
-    for (int it = 0; it < kWaitTries; ++it)
+    for (int it = 0; it < tries; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     if (err) *(volatile unsigned*)err = kErrWaitTimeout;   // plain store: err may be host-mapped
     return false;

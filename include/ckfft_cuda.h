@@ -175,6 +175,16 @@ int CkFftCudaStft(CkFftContext* context, int n, long long frames, const float* s
 int CkFftCudaFilterInverse(CkFftContext* context, int n, long long frames, const CkFftComplex* spectra,
                            const CkFftComplex* filter, float scale, float* output, void* stream);
 
+/* Self-test of the library's failure detection: makes one of its bounded
+ * device-side waits run out on purpose -- which = 0: a mixed-run phase unit
+ * waiting for a completion counter that nothing increments; which = 1: a wait
+ * for a bulk copy that never arrives -- and checks that the kernel reported
+ * the timeout through the error word, returned, and left the context able to
+ * transform (a 64-point check).  Nothing faults or hangs; each wait is
+ * bounded to about a millisecond here.  Returns 1 when all of that held,
+ * else 0 with CkFftCudaGetLastError() saying what did not. */
+int CkFftCudaSelfTestWait(CkFftContext* context, int which);
+
 /* Number of kernel launches the library has issued in this process (all
  * contexts, all threads).  Lets a caller count launches inside a timed region. */
 long long CkFftCudaLaunchCount(void);
