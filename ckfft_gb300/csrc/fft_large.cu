@@ -57,6 +57,27 @@ k_rows(const float2* __restrict__ in, float2* __restrict__ out, long long count,
                                                     threadIdx.x, smem, tw);
 }
 
+// Third pass of the three-pass transform (N = N1 N2 N3, sub-lengths 2^l1,
+// 2^l2, 2^LB): block (f, k2, tile) runs DFT_N3 along the C rows k1 of the
+// tile, row (k1, k2) of transform f at in[f N + k1 N2 N3 + k2 N3 ..], and
+// stores X[k1 + N1 k2 + N1 N2 k3] -- C consecutive outputs per k3.
+template <int LB, bool INV>
+__global__ void __launch_bounds__(BPass<LB>::THREADS)
+k_rows3(const float2* __restrict__ in, float2* __restrict__ out, int l1, int l2, long long out_dist,
+        const float2* __restrict__ tw)
+{
+    using P = BPass<LB>;
+    extern __shared__ float2 smem[];
+    const long long tiles = (1ll << l1) / P::C;
+    const long long b = blockIdx.x;
+    const long long tile = b % tiles;
+    const long long k2 = (b / tiles) & ((1ll << l2) - 1);
+    const long long f = b / (tiles << l2);
+    const long long n = 1ll << (l1 + l2 + LB);
+    pass_rows<LB, INV, false, BatchMaxT<LB>::value>(in + f * n + (k2 << LB), out + f * out_dist + (k2 << l1),
+                                                    l1 + l2, tile, threadIdx.x, smem, tw, true, l2 + LB);
+}
+
 // ------------------------------------------------- real split / merge passes
 
 // In-place split of a natural-order half-length spectrum Z (M = 2^lm values,
@@ -132,6 +153,70 @@ static cudaError_t launch_rows(int lb, const float2* in, float2* out, long long 
     CKG_SUB_SWITCH(lb, launch_rows_L, in, out, count, log2n1, in_dist, out_dist, tw, s)
 }
 
+template <int LB, bool INV>
+static cudaError_t launch_rows3_L(const float2* in, float2* out, long long count, int l1, int l2, long long out_dist,
+                                  const float2* tw, cudaStream_t s)
+{
+    using P = BPass<LB>;
+    const long long blocks = count * ((1ll << l1) / P::C) << l2;
+    k_rows3<LB, INV><<<(unsigned)blocks, P::THREADS, P::SMEM, s>>>(in, out, l1, l2, out_dist, tw);
+    return cudaGetLastError();
+}
+
+template <bool INV>
+static cudaError_t launch_rows3(int l3, const float2* in, float2* out, long long count, int l1, int l2,
+                                long long out_dist, const float2* tw, cudaStream_t s)
+{
+    switch (l3) {
+    case 7: return launch_rows3_L<7, INV>(in, out, count, l1, l2, out_dist, tw, s);
+    case 8: return launch_rows3_L<8, INV>(in, out, count, l1, l2, out_dist, tw, s);
+    case 9: return launch_rows3_L<9, INV>(in, out, count, l1, l2, out_dist, tw, s);
+    case 10: return launch_rows3_L<10, INV>(in, out, count, l1, l2, out_dist, tw, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// Three sub-lengths of at most 2^10 (each >= 2^7), as equal as possible.
+static bool plan3(int log2n, int* l1, int* l2, int* l3)
+{
+    if (log2n < 21 || log2n > 30) return false;
+    *l3 = (log2n + 2) / 3;
+    *l2 = (log2n - *l3 + 1) / 2;
+    *l1 = log2n - *l3 - *l2;
+    return *l1 >= 7 && *l3 <= 10 && *l2 <= 10;
+}
+
+// Sizes from 2^kThreePassMinLog2 on run as three passes whose tiles are all
+// 16 columns / rows wide (128-byte accesses); two passes there would need
+// sub-lengths above 2^10, whose tiles are 4 or 8 wide.
+constexpr int kThreePassMinLog2 = 21;
+
+static cudaError_t launch_three_pass(bool inverse, int log2n, const float2* in, float2* out, long long count,
+                                     long long in_dist, long long out_dist, const float2* tw, float2* tmp,
+                                     long long group, cudaStream_t s)
+{
+    int l1, l2, l3;
+    if (!plan3(log2n, &l1, &l2, &l3)) return cudaErrorInvalidValue;
+    const long long n = 1ll << log2n, M = 1ll << (l2 + l3);
+    for (long long off = 0; off < count; off += group) {
+        const long long cnt = count - off < group ? count - off : group;
+        // pass 1: columns of length N1 over the M = N2 N3 columns -> tmp
+        cudaError_t e = inverse ? launch_cols<true>(l1, in + off * in_dist, tmp, cnt, l2 + l3, in_dist, n, tw, s)
+                                : launch_cols<false>(l1, in + off * in_dist, tmp, cnt, l2 + l3, in_dist, n, tw, s);
+        // pass 2: in every row k1, columns of length N2 over the N3 columns, in place
+        if (e == cudaSuccess)
+            e = inverse ? launch_cols<true>(l2, tmp, tmp, cnt << l1, l3, M, M, tw, s)
+                        : launch_cols<false>(l2, tmp, tmp, cnt << l1, l3, M, M, tw, s);
+        // pass 3: rows of length N3, C consecutive k1 per tile -> out
+        if (e == cudaSuccess)
+            e = inverse ? launch_rows3<true>(l3, tmp, out + off * out_dist, cnt, l1, l2, out_dist, tw, s)
+                        : launch_rows3<false>(l3, tmp, out + off * out_dist, cnt, l1, l2, out_dist, tw, s);
+        if (e != cudaSuccess) return e;
+        count_launch(3);
+    }
+    return cudaSuccess;
+}
+
 LargePlan large_plan(int log2n)
 {
     LargePlan p;
@@ -171,6 +256,8 @@ cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out,
     const float2* src = (const float2*)in;
     float2* dst = (float2*)out;
     float2* tmp = (float2*)scratch;
+    if (log2n >= kThreePassMinLog2 && ((uintptr_t)scratch & 127) == 0)
+        return launch_three_pass(inverse, log2n, src, dst, count, in_dist, out_dist, tw, tmp, group, s);
     for (long long off = 0; off < count; off += group) {
         const long long cnt = count - off < group ? count - off : group;
         cudaError_t e = inverse
@@ -228,6 +315,10 @@ static cudaError_t attr_pass()
 {
     using P = BPass<L>;
     cudaError_t e;
+    if constexpr (L <= 10) {
+        if ((e = cudaFuncSetAttribute(k_rows3<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
+        if ((e = cudaFuncSetAttribute(k_rows3<L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
+    }
     if ((e = cudaFuncSetAttribute(k_cols<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(k_cols<L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(k_rows<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;

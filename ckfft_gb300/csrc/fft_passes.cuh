@@ -118,17 +118,20 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
 // Row pass for tile `tile` (rows tile*C .. tile*C+C-1) of one transform.
 // DISCARD: the input is a dead intermediate (scratch) whose L2 lines may be
 // dropped without write-back once read; it must be 128-byte aligned.
+// log2_row_stride: distance between consecutive rows of the input (default:
+// the row length, rows back to back).
 template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true>
 __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
                                           long long tile, int tid, float2* smem, const float2* __restrict__ tw,
-                                          bool live = true)
+                                          bool live = true, int log2_row_stride = LB)
 {
     using P = PassCfg<LB, MAXT>;
     constexpr int N2 = 1 << LB;
     const int r = tid / P::T, t = tid % P::T;
     const long long n1len = 1ll << log2n1;
     const long long row0 = tile * P::C;
-    const float2* src = in + (row0 + r) * N2 + t;
+    const long long rstride = 1ll << log2_row_stride;
+    const float2* src = in + (row0 + r) * rstride + t;
     float2 v[P::R];
 #pragma unroll
     for (int m = 0; m < P::R; ++m) v[m] = live ? ld_data<CG>(src + m * P::T) : make_float2(0.f, 0.f);
@@ -139,7 +142,7 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
         // every thread of the tile has consumed its inputs: the intermediate
         // rows are dead, so drop their L2 lines instead of writing them back
         static_assert(N2 % 16 == 0, "rows span whole 128-byte lines");
-        const char* row = (const char*)(in + (row0 + r) * N2);
+        const char* row = (const char*)(in + (row0 + r) * rstride);
 #pragma unroll
         for (int l = t; l < N2 / 16; l += P::T)
             asm volatile("discard.global.L2 [%0], 128;" ::"l"(row + 128 * l) : "memory");

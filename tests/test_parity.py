@@ -178,9 +178,10 @@ def test_real_sizes_vs_oracle(torch_cuda, ctx_cache, oracle_mod, l2):
             assert_close(got_i[f], ri, n, f"rinv n=2^{l2}")
 
 
-@pytest.mark.parametrize("l2", [22, 24])
+@pytest.mark.parametrize("l2", [21, 22, 23, 24])
 def test_large_complex_vs_oracle_and_fp64(torch_cuda, ctx_cache, oracle_mod, l2):
-    """Workload 3 sizes: N(0,1) inputs, forward and inverse."""
+    """Workload 3 sizes (and the three-pass sizes between): N(0,1) inputs,
+    forward and inverse."""
     n = 1 << l2
     rng = np.random.default_rng(300 + l2)
     x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
@@ -190,6 +191,29 @@ def test_large_complex_vs_oracle_and_fp64(torch_cuda, ctx_cache, oracle_mod, l2)
         got = run_batch(torch_cuda, ctx, kind, n, x[None])[0]
         assert_close(got, o.complex(n, x, inv), n, f"{kind} 2^{l2}")
         assert rel_l2(got, oracle_mod.fp64_complex(x, inv)) < 2e-6
+
+
+@pytest.mark.parametrize("kind,l2,count", [("cfwd", 21, 3), ("cinv", 22, 2), ("rfwd", 22, 2), ("rinv", 23, 2)])
+def test_three_pass_batches(torch_cuda, ctx_cache, oracle_mod, kind, l2, count):
+    """Batches on the three-pass path: every transform against the oracle."""
+    n = 1 << l2
+    rng = np.random.default_rng(400 + l2)
+    m = n // 2 + 1 if kind == "rinv" else n
+    if kind == "rfwd":
+        x = rng.standard_normal((count, n)).astype(np.float32)
+    else:
+        x = (rng.standard_normal((count, m)) + 1j * rng.standard_normal((count, m))).astype(np.complex64)
+    o = oracle_mod.Oracle(n)
+    ctx = ctx_cache(n)
+    got = run_batch(torch_cuda, ctx, kind, n, x)
+    for f in range(count):
+        if kind == "rfwd":
+            ref = o.real_forward(n, x[f])
+        elif kind == "rinv":
+            ref = o.real_inverse(n, x[f])
+        else:
+            ref = o.complex(n, x[f], kind == "cinv")
+        assert_close(got[f], ref, n, f"{kind} 2^{l2} frame {f}")
 
 
 # ------------------------------------------------- pipelined kernels + tails
