@@ -1,5 +1,5 @@
-// fft_l2pass.cu -- complex 2^15 and 2^16 in two passes whose intermediate
-// never reaches HBM.
+// fft_l2pass.cu -- complex 2^15 and 2^16 (and real 2^16, 2^17) in two
+// passes whose intermediate never reaches HBM.
 //
 // The multi-pass transform of fft_large.cu (columns, then rows, see
 // fft_passes.cuh) runs here inside one thread-block cluster of K CTAs per
@@ -13,7 +13,10 @@
 // on GB300 (batches of 1 GiB): 2^15 3328 vs 3145 GB/s, 2^16 3439 vs 3105;
 // the kernel is then bound by the two passes' instructions, not by HBM (40 %
 // DRAM throughput, no intermediate bytes in DRAM).  At 2^17 it was slower
-// (2779 vs 2857) and is not used there.
+// (2779 vs 2857) and is not used there.  Real 2^16 / 2^17 run the split or
+// merge as a third phase of the same cluster: forward 2090 / 2183 vs 2055 /
+// 2037 GB/s with a separate split kernel, inverse 2355 / 2444 vs 1878 / 1835
+// with a separate merge kernel.
 #include <cooperative_groups.h>
 
 #include "fft_passes.cuh"
@@ -43,15 +46,88 @@ struct L2Cfg {
     static_assert(ITER_B >= 1 && ITER_B * kL2Cluster * SGB == TILES_B, "row tiles split evenly");
 };
 
-// One transform per cluster: blockIdx.x / K.  scratch holds n values per
-// transform of the launch (128-byte aligned rows).
-template <int LA, int LB, bool INV>
+__device__ __forceinline__ void cluster_barrier(cg::cluster_group& cluster)
+{
+    // global stores before the barrier are seen by the peers' loads after it:
+    // the cluster barrier releases and acquires at cluster scope; the fence
+    // makes the ordering of the global stores explicit
+    asm volatile("fence.acq_rel.cluster;" ::: "memory");
+    cluster.sync();
+}
+
+// The real forward split of a whole half-length spectrum y (n values, room
+// for n+1) by the cluster's CT threads, idx = this thread's rank: pair k
+// (k = 0 .. n/2) gives bins k and n-k, the algebra of split_pair_inplace.
+// Each thread first loads a batch of its pairs (they come from L2), then
+// computes and stores them, so the loads are in flight together.
+template <long long N, int CT>
+__device__ __forceinline__ void split_phase(float2* __restrict__ y, int idx, const float2* __restrict__ twn)
+{
+    constexpr int PER = (int)((N / 2 + CT) / CT);
+    constexpr int B = 8;
+#pragma unroll 1
+    for (int j0 = 0; j0 < PER; j0 += B) {
+        float2 a[B], b[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const long long k = idx + (long long)(j0 + j) * CT;
+            if (j0 + j < PER && k <= N / 2) {
+                a[j] = __ldcg(y + k);
+                b[j] = __ldcg(y + ((N - k) & (N - 1)));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const long long k = idx + (long long)(j0 + j) * CT;
+            if (j0 + j < PER && k <= N / 2) {
+                y[k] = real_split(a[j], b[j], __ldg(twn + k));
+                if (k != N / 2) y[N - k] = real_split(b[j], a[j], __ldg(twn + (N - k)));
+            }
+        }
+    }
+}
+
+// The real inverse merge of n+1 bins x into n values s (merge_elem's algebra).
+template <long long N, int CT>
+__device__ __forceinline__ void merge_phase(const float2* __restrict__ x, float2* __restrict__ s, int idx,
+                                            const float2* __restrict__ twn)
+{
+    constexpr int PER = (int)(N / CT);
+    constexpr int B = 8;
+#pragma unroll 1
+    for (int j0 = 0; j0 < PER; j0 += B) {
+        float2 a[B], b[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const long long k = idx + (long long)(j0 + j) * CT;
+            a[j] = __ldcs(x + k);
+            b[j] = __ldg(x + (N - k));
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const long long k = idx + (long long)(j0 + j) * CT;
+            s[k] = real_merge(a[j], b[j], __ldg(twn + k));
+        }
+    }
+}
+
+// One transform per cluster: blockIdx.x / K.  scratch holds 2^(LA+LB) values
+// per transform of the launch (128-byte aligned rows).
+// KIND 0 / 1: complex forward / inverse of n = 2^(LA+LB) points.
+// KIND 2: real forward of 2n reals (read as n packed pairs; in_dist in pairs):
+//         the complex forward, then the split of the half-length spectrum in
+//         place on the output (n+1 bins), a third phase inside the cluster.
+// KIND 3: real inverse to 2n reals (out_dist in pairs): the merge of the n+1
+//         bins into the intermediate first, then the complex inverse.
+template <int LA, int LB, int KIND>
 __global__ void __cluster_dims__(kL2Cluster, 1, 1) __launch_bounds__(kL2Threads, 4)
 k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __restrict__ scratch, long long in_dist,
          long long out_dist, const float2* __restrict__ tw)
 {
     using C = L2Cfg<LA, LB>;
+    constexpr bool INV = KIND == 1 || KIND == 3;
     constexpr long long n = 1ll << (LA + LB);
+    constexpr int CT = kL2Cluster * kL2Threads;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const long long f = blockIdx.x / kL2Cluster;
@@ -59,45 +135,57 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     const float2* x = in + f * in_dist;
     float2* y = out + f * out_dist;
     float2* s = scratch + f * n;
+    const float2* twn = tw + 2 * n;                  // W_(2n): split / merge twiddles
 
+    if constexpr (KIND == 3) {
+        merge_phase<n, CT>(x, s, rank * kL2Threads + threadIdx.x, twn);
+        cluster_barrier(cluster);
+    }
+    // columns: the input (or, real inverse, the merged spectrum in place) -> s
+    const float2* src = KIND == 3 ? s : x;
     const int sga = threadIdx.x / C::PA::THREADS, ta = threadIdx.x % C::PA::THREADS;
 #pragma unroll 1
     for (int i = 0; i < C::ITER_A; ++i) {
         const int tile = (i * kL2Cluster + rank) * C::SGA + sga;
-        pass_cols<LA, INV, false, kL2Threads>(x, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
+        pass_cols<LA, INV, KIND == 3, kL2Threads>(src, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
         __syncthreads();                             // the tile's shared memory is reused
     }
-    // every column tile of the transform is in L2 before any row tile reads
-    // it: the cluster barrier releases and acquires at cluster scope; the
-    // fence makes the ordering of the global stores explicit
-    asm volatile("fence.acq_rel.cluster;" ::: "memory");
-    cluster.sync();
+    // every column tile of the transform is in L2 before any row tile reads it
+    cluster_barrier(cluster);
     const int sgb = threadIdx.x / C::PB::THREADS, tb = threadIdx.x % C::PB::THREADS;
 #pragma unroll 1
     for (int i = 0; i < C::ITER_B; ++i) {
         const int tile = (i * kL2Cluster + rank) * C::SGB + sgb;
-        pass_rows<LB, INV, true, kL2Threads, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, tw);
+        pass_rows<LB, INV, true, kL2Threads, true, KIND != 2>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, tw);
         __syncthreads();
+    }
+    if constexpr (KIND == 2) {
+        // split in place: the half-length spectrum was just written (in L2)
+        cluster_barrier(cluster);
+        split_phase<n, CT>(y, rank * kL2Threads + threadIdx.x, twn);
+        // peers of this CTA may still read the lines it wrote; nothing else
+        // is shared, so the CTAs may leave independently
     }
 }
 
-template <int LA, int LB, bool INV>
+template <int LA, int LB, int KIND>
 static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, long long count, long long in_dist,
                                long long out_dist, const float2* tw, cudaStream_t s)
 {
     using C = L2Cfg<LA, LB>;
-    k_l2_c2c<LA, LB, INV><<<(unsigned)(count * kL2Cluster), kL2Threads, C::SMEM, s>>>(in, out, scratch, in_dist,
-                                                                                    out_dist, tw);
+    k_l2_c2c<LA, LB, KIND><<<(unsigned)(count * kL2Cluster), kL2Threads, C::SMEM, s>>>(in, out, scratch, in_dist,
+                                                                                     out_dist, tw);
     return cudaGetLastError();
 }
 
 bool l2pass_supported(int log2n) { return log2n >= 15 && log2n <= 16; }
 
-cudaError_t launch_l2pass_c2c(bool inverse, int log2n, const void* in, void* out, long long count, long long in_dist,
-                              long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes,
-                              cudaStream_t s)
+// kind: 0 / 1 complex forward / inverse, 2 / 3 real forward / inverse whose
+// half length is 2^log2n (dists in complex units / packed pairs).
+cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,
+                          long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
-    if (!l2pass_supported(log2n)) return cudaErrorInvalidValue;
+    if (!l2pass_supported(log2n) || kind < 0 || kind > 3) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;
     const long long n = 1ll << log2n;
     const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
@@ -110,13 +198,16 @@ cudaError_t launch_l2pass_c2c(bool inverse, int log2n, const void* in, void* out
         const float2* a = src + off * in_dist;
         float2* b = dst + off * out_dist;
         cudaError_t e;
-        switch (log2n) {
-        case 15: e = inverse ? launch_l2_L<7, 8, true>(a, b, tmp, cnt, in_dist, out_dist, tw, s)
-                             : launch_l2_L<7, 8, false>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;
-        case 16: e = inverse ? launch_l2_L<8, 8, true>(a, b, tmp, cnt, in_dist, out_dist, tw, s)
-                             : launch_l2_L<8, 8, false>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;
-        default: e = cudaErrorInvalidValue;
-        }
+#define CKG_L2_KIND(LA, LB)                                                                        \
+    switch (kind) {                                                                                \
+    case 0: e = launch_l2_L<LA, LB, 0>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
+    case 1: e = launch_l2_L<LA, LB, 1>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
+    case 2: e = launch_l2_L<LA, LB, 2>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
+    default: e = launch_l2_L<LA, LB, 3>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;          \
+    }
+        if (log2n == 15) { CKG_L2_KIND(7, 8) }
+        else { CKG_L2_KIND(8, 8) }
+#undef CKG_L2_KIND
         if (e != cudaSuccess) return e;
         count_launch();
     }
@@ -127,9 +218,11 @@ template <int LA, int LB>
 static cudaError_t attr_l2()
 {
     const int smem = (int)L2Cfg<LA, LB>::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 0>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 1>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 2>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 3>, a, smem);
     return e;
 }
 

@@ -248,7 +248,7 @@ cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out,
     // 2^15, 2^16: both passes inside one cluster per transform, the
     // intermediate kept in L2 (fft_l2pass.cu)
     if (l2pass_supported(log2n) && ((uintptr_t)scratch & 127) == 0)
-        return launch_l2pass_c2c(inverse, log2n, in, out, count, in_dist, out_dist, tw, scratch, scratch_bytes, s);
+        return launch_l2pass(inverse ? 1 : 0, log2n, in, out, count, in_dist, out_dist, tw, scratch, scratch_bytes, s);
     const LargePlan p = large_plan(log2n);
     const long long n = 1ll << log2n;
     const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
@@ -280,6 +280,8 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
     // in: n floats per frame (n/2 packed complex), out: n/2+1 complex per frame
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
+    if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0 && scratch_bytes >= sizeof(float2) * (size_t)M)
+        return launch_l2pass(2, lm, in, out, count, in_dist / 2, out_dist, tw, scratch, scratch_bytes, s);
     cudaError_t e = launch_large_c2c(false, lm, in, out, count, in_dist / 2, out_dist, tw, scratch,
                                      scratch_bytes, s);
     if (e != cudaSuccess) return e;
@@ -298,6 +300,8 @@ cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long cou
     // in: n/2+1 complex per frame, out: n floats per frame (n/2 packed complex)
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
+    if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0 && scratch_bytes >= sizeof(float2) * (size_t)M)
+        return launch_l2pass(3, lm, in, out, count, in_dist, out_dist / 2, tw, scratch, scratch_bytes, s);
     const long long work = count * M;
     const int threads = 256;
     k_merge<<<(unsigned)((work + threads - 1) / threads), threads, 0, s>>>(

@@ -120,7 +120,9 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
 // dropped without write-back once read; it must be 128-byte aligned.
 // log2_row_stride: distance between consecutive rows of the input (default:
 // the row length, rows back to back).
-template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true>
+// STREAM: outputs stored with the evict-first hint (false: they are read
+// again soon, by a later phase of the same kernel).
+template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true, bool STREAM = true>
 __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
                                           long long tile, int tid, float2* smem, const float2* __restrict__ tw,
                                           bool live = true, int log2_row_stride = LB)
@@ -157,7 +159,8 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
 #pragma unroll
     for (int m = 0; m < P::R; ++m) {
         const int k2 = t2 + m * P::T;
-        __stcs(dst + (long long)k2 * n1len, smem[TileView<P::C>::slot(k2, r2)]);
+        if constexpr (STREAM) __stcs(dst + (long long)k2 * n1len, smem[TileView<P::C>::slot(k2, r2)]);
+        else dst[(long long)k2 * n1len] = smem[TileView<P::C>::slot(k2, r2)];
     }
 }
 
