@@ -412,19 +412,23 @@ def l2_flusher(torch, dev):
 
 
 def timed_steps(torch, stream, step, steps, flush=None):
-    """Per-step CUDA-event time on `stream` (flush, if any, runs outside the events)."""
-    total = 0.0
-    for _ in range(steps):
-        if flush:
-            flush()
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        step()
-        b.record(stream)
-        torch.cuda.synchronize()
-        total += a.elapsed_time(b) / 1e3
-    return total
+    """Sum of per-step CUDA-event times on `stream`.  Every step and every L2
+    flush (between steps, outside the events) is enqueued on `stream` ahead
+    of time, so the events time the GPU's work rather than the host's calls;
+    one synchronize closes the run."""
+    torch.cuda.synchronize()
+    events = []
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            if flush:
+                flush()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            events.append((a, b))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in events) / 1e3
 
 
 def base_line(args, metric, value, unit, secs, config, world=1):
