@@ -11,9 +11,8 @@
 //
 // Covered: complex 2^6 .. 2^13 (either side or both interleaved), real
 // forward with interleaved reals, real inverse with interleaved reals, real
-// n = 2^7 .. 2^14.  G = max(4, frames per CTA of the batched shape) up to
-// 2^12 (rows of 32 bytes and more), G = 2 at 2^13 (two 512-thread
-// transforms, 1024 threads).
+// n = 2^7 .. 2^14.  G is at least 16 (rows of 128 bytes and more) up to
+// 2^10, then 8, 4 and 2 transforms per 1024-thread CTA at 2^11, 2^12, 2^13.
 #include "fft_small.cuh"
 
 namespace ckg {
@@ -22,7 +21,9 @@ template <int L>
 struct InterCfg {
     using S = SmallCfg<L>;
     static constexpr int LOG2R = S::LOG2R, R = S::R, T = S::T;
-    static constexpr int G = S::TPB >= 4 ? S::TPB : (L <= 12 ? 4 : 2);
+    // transforms per CTA: rows of at least 128 bytes (G >= 16) where 1024
+    // threads and the shared memory allow, else 4 (2 at 2^13)
+    static constexpr int G = S::TPB >= 16 ? S::TPB : L <= 10 ? 16 : L == 11 ? 8 : L == 12 ? 4 : 2;
     static constexpr int THREADS = T * G;
     static constexpr int MINB = 1024 / THREADS > 0 ? 1024 / THREADS : 1;
     static constexpr bool WARP = S::WARP;
@@ -283,6 +284,7 @@ static cudaError_t attr_inter()
 cudaError_t prepare_inter()
 {
     cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = attr_inter<9>();
     if (e == cudaSuccess) e = attr_inter<10>();
     if (e == cudaSuccess) e = attr_inter<11>();
     if (e == cudaSuccess) e = attr_inter<12>();
