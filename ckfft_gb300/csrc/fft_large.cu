@@ -28,8 +28,16 @@ template <int LS>
 struct BatchMaxT {
     static constexpr int value = LS > 10 ? 1024 : 512;
 };
+// Widest tile of the batched passes: 16 sequences (128-byte row accesses).
+// 32 (256-byte rows) up to sub-length 2^8 measured slower on GB300: batched
+// 2^17 2604 vs 2740 GB/s, 2^24 1723 vs 1942 (twice the shared memory per
+// CTA, half the CTAs per SM).
 template <int LS>
-using BPass = PassCfg<LS, BatchMaxT<LS>::value>;
+struct BatchCMax {
+    static constexpr int value = 16;
+};
+template <int LS>
+using BPass = PassCfg<LS, BatchMaxT<LS>::value, BatchCMax<LS>::value>;
 
 template <int LA, bool INV>
 __global__ void __launch_bounds__(BPass<LA>::THREADS)
@@ -40,8 +48,8 @@ k_cols(const float2* __restrict__ in, float2* __restrict__ out, long long count,
     extern __shared__ float2 smem[];
     const long long tiles = (1ll << log2n2) / P::C;
     const long long f = blockIdx.x / tiles;
-    pass_cols<LA, INV, false, BatchMaxT<LA>::value>(in + f * in_dist, out + f * out_dist, log2n2, blockIdx.x % tiles,
-                                                    threadIdx.x, smem, tw);
+    pass_cols<LA, INV, false, BatchMaxT<LA>::value, BatchCMax<LA>::value>(in + f * in_dist, out + f * out_dist, log2n2,
+                                                                          blockIdx.x % tiles, threadIdx.x, smem, tw);
 }
 
 template <int LB, bool INV>
@@ -53,8 +61,8 @@ k_rows(const float2* __restrict__ in, float2* __restrict__ out, long long count,
     extern __shared__ float2 smem[];
     const long long tiles = (1ll << log2n1) / P::C;
     const long long f = blockIdx.x / tiles;
-    pass_rows<LB, INV, false, BatchMaxT<LB>::value>(in + f * in_dist, out + f * out_dist, log2n1, blockIdx.x % tiles,
-                                                    threadIdx.x, smem, tw);
+    pass_rows<LB, INV, false, BatchMaxT<LB>::value, true, true, BatchCMax<LB>::value>(
+        in + f * in_dist, out + f * out_dist, log2n1, blockIdx.x % tiles, threadIdx.x, smem, tw);
 }
 
 // Third pass of the three-pass transform (N = N1 N2 N3, sub-lengths 2^l1,
@@ -74,8 +82,8 @@ k_rows3(const float2* __restrict__ in, float2* __restrict__ out, int l1, int l2,
     const long long k2 = (b / tiles) & ((1ll << l2) - 1);
     const long long f = b / (tiles << l2);
     const long long n = 1ll << (l1 + l2 + LB);
-    pass_rows<LB, INV, false, BatchMaxT<LB>::value>(in + f * n + (k2 << LB), out + f * out_dist + (k2 << l1),
-                                                    l1 + l2, tile, threadIdx.x, smem, tw, true, l2 + LB);
+    pass_rows<LB, INV, false, BatchMaxT<LB>::value, true, true, BatchCMax<LB>::value>(
+        in + f * n + (k2 << LB), out + f * out_dist + (k2 << l1), l1 + l2, tile, threadIdx.x, smem, tw, true, l2 + LB);
 }
 
 // ------------------------------------------------- real split / merge passes

@@ -21,12 +21,13 @@ namespace ckg {
 // 512 threads, sub-lengths above 2^10 take 32 values per thread (128
 // registers); with 1024 threads they keep 16 values (64 registers) and twice
 // the resident warps.
-template <int LS, int MAXT = 512>
+// CMAX: widest tile (C * 8 bytes per row access).
+template <int LS, int MAXT = 512, int CMAX = 16>
 struct PassCfg {
     static constexpr int LOG2R = LS < 4 ? LS : (LS <= 10 || MAXT >= 1024) ? 4 : 5;
     static constexpr int R = 1 << LOG2R;
     static constexpr int T = (1 << LS) / R;
-    static constexpr int C = MAXT / T < 16 ? MAXT / T : 16;
+    static constexpr int C = MAXT / T < CMAX ? MAXT / T : CMAX;
     static constexpr int THREADS = C * T;
     // interleaved (pass 1 and pass-2 transpose) and per-row padded (pass 2) layouts
     static constexpr int INTERLEAVED = (1 << LS) * C + ((1 << LS) * C >> 4) + 1;
@@ -69,12 +70,12 @@ __device__ __forceinline__ float2 big_twiddle(const float2* __restrict__ tw, int
 // Column pass for tile `tile` of one transform, by threads tid = 0..THREADS-1.
 // live == false: the threads take part in the barriers only (no memory
 // access outside the tile's shared memory).
-template <int LA, bool INV, bool CG, int MAXT = 512>
+template <int LA, bool INV, bool CG, int MAXT = 512, int CMAX = 16>
 __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
                                           long long tile, int tid, float2* smem, const float2* __restrict__ tw,
                                           bool live = true)
 {
-    using P = PassCfg<LA, MAXT>;
+    using P = PassCfg<LA, MAXT, CMAX>;
     const int c = tid % P::C, t = tid / P::C;
     const long long n2len = 1ll << log2n2;
     const long long n2 = tile * P::C + c;
@@ -122,12 +123,12 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
 // the row length, rows back to back).
 // STREAM: outputs stored with the evict-first hint (false: they are read
 // again soon, by a later phase of the same kernel).
-template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true, bool STREAM = true>
+template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true, bool STREAM = true, int CMAX = 16>
 __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
                                           long long tile, int tid, float2* smem, const float2* __restrict__ tw,
                                           bool live = true, int log2_row_stride = LB)
 {
-    using P = PassCfg<LB, MAXT>;
+    using P = PassCfg<LB, MAXT, CMAX>;
     constexpr int N2 = 1 << LB;
     const int r = tid / P::T, t = tid % P::T;
     const long long n1len = 1ll << log2n1;
