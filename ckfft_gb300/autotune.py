@@ -117,7 +117,7 @@ def write_outputs(results: dict, out_dir: str, gpu: str) -> None:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--out-dir", default=".", help="where autotune.json / autotune.md are written")
     ap.add_argument("--mb", type=int, default=256)
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--measure", action="store_true", help=argparse.SUPPRESS)
