@@ -1,7 +1,7 @@
 """ctypes front end for the CPU oracle and for the reference build (test infrastructure).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this module.
-It is the checker, never the product: the product library is
+It checks results and is never the product: the product library is
 ckfft_gb300/libckfft_cuda.so and it has no CPU path.
 
 Three back ends share one small interface (`complex`, `real_forward`,
