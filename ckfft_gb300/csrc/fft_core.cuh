@@ -207,6 +207,19 @@ __device__ __forceinline__ void xsync()
     else __syncthreads();
 }
 
+// ---------------------------------------- programmatic dependent launch
+// A kernel launched by launch_pdl() may be scheduled while the kernel before
+// it in the stream is still finishing (sm_90+).  Each such kernel calls
+// pdl_start() first: it lets the next kernel begin to launch, then waits
+// until the previous one has completed and its writes are visible, before
+// any memory access.  After a kernel that never signals, the wait returns at
+// once: the launch then behaves like a plain one.
+__device__ __forceinline__ void pdl_start()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // ------------------------------------------------------- Stockham engine
 
 // Stage s has radix 2^lrs(s) and span 2^lns(s).  The full radix goes first,

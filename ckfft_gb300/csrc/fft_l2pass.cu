@@ -132,6 +132,7 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     const int rank = (int)cluster.block_rank();
     const long long f = blockIdx.x / kL2Cluster;
     extern __shared__ __align__(128) float2 smem[];
+    pdl_start();
     const float2* x = in + f * in_dist;
     float2* y = out + f * out_dist;
     float2* s = scratch + f * n;
@@ -173,9 +174,8 @@ static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, l
                                long long out_dist, const float2* tw, cudaStream_t s)
 {
     using C = L2Cfg<LA, LB>;
-    k_l2_c2c<LA, LB, KIND><<<(unsigned)(count * kL2Cluster), kL2Threads, C::SMEM, s>>>(in, out, scratch, in_dist,
-                                                                                     out_dist, tw);
-    return cudaGetLastError();
+    return launch_pdl(k_l2_c2c<LA, LB, KIND>, dim3((unsigned)(count * kL2Cluster)), dim3(kL2Threads), C::SMEM, s, in,
+                      out, scratch, in_dist, out_dist, tw);
 }
 
 bool l2pass_supported(int log2n) { return log2n >= 15 && log2n <= 16; }

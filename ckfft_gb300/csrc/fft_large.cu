@@ -46,6 +46,7 @@ k_cols(const float2* __restrict__ in, float2* __restrict__ out, long long count,
 {
     using P = BPass<LA>;
     extern __shared__ float2 smem[];
+    pdl_start();
     const long long tiles = (1ll << log2n2) / P::C;
     const long long f = blockIdx.x / tiles;
     pass_cols<LA, INV, false, BatchMaxT<LA>::value, BatchCMax<LA>::value>(in + f * in_dist, out + f * out_dist, log2n2,
@@ -59,6 +60,7 @@ k_rows(const float2* __restrict__ in, float2* __restrict__ out, long long count,
 {
     using P = BPass<LB>;
     extern __shared__ float2 smem[];
+    pdl_start();
     const long long tiles = (1ll << log2n1) / P::C;
     const long long f = blockIdx.x / tiles;
     pass_rows<LB, INV, false, BatchMaxT<LB>::value, true, true, BatchCMax<LB>::value>(
@@ -76,6 +78,7 @@ k_rows3(const float2* __restrict__ in, float2* __restrict__ out, int l1, int l2,
 {
     using P = BPass<LB>;
     extern __shared__ float2 smem[];
+    pdl_start();
     const long long tiles = (1ll << l1) / P::C;
     const long long b = blockIdx.x;
     const long long tile = b % tiles;
@@ -93,6 +96,7 @@ k_rows3(const float2* __restrict__ in, float2* __restrict__ out, int l1, int l2,
 __global__ void k_split_inplace(float2* __restrict__ z, long long count, int lm, long long dist,
                                 const float2* __restrict__ tw)
 {
+    pdl_start();
     const long long M = 1ll << lm;
     const long long per = M / 2 + 1;                 // pairs (k, M-k) for k = 0..M/2
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,6 +109,7 @@ __global__ void k_split_inplace(float2* __restrict__ z, long long count, int lm,
 __global__ void k_merge(const float2* __restrict__ x, float2* __restrict__ y, long long count, int lm,
                         long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
+    pdl_start();
     const long long M = 1ll << lm;
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= count * M) return;
@@ -120,8 +125,8 @@ static cudaError_t launch_cols_L(const float2* in, float2* out, long long count,
 {
     using P = BPass<LA>;
     const long long blocks = count * ((1ll << log2n2) / P::C);
-    k_cols<LA, INV><<<(unsigned)blocks, P::THREADS, P::SMEM, s>>>(in, out, count, log2n2, in_dist, out_dist, tw);
-    return cudaGetLastError();
+    return launch_pdl(k_cols<LA, INV>, dim3((unsigned)blocks), dim3(P::THREADS), P::SMEM, s, in, out, count, log2n2,
+                      in_dist, out_dist, tw);
 }
 
 template <int LB, bool INV>
@@ -130,8 +135,8 @@ static cudaError_t launch_rows_L(const float2* in, float2* out, long long count,
 {
     using P = BPass<LB>;
     const long long blocks = count * ((1ll << log2n1) / P::C);
-    k_rows<LB, INV><<<(unsigned)blocks, P::THREADS, P::SMEM, s>>>(in, out, count, log2n1, in_dist, out_dist, tw);
-    return cudaGetLastError();
+    return launch_pdl(k_rows<LB, INV>, dim3((unsigned)blocks), dim3(P::THREADS), P::SMEM, s, in, out, count, log2n1,
+                      in_dist, out_dist, tw);
 }
 
 #define CKG_SUB_SWITCH(L, FN, ...)                                                                 \
@@ -167,8 +172,8 @@ static cudaError_t launch_rows3_L(const float2* in, float2* out, long long count
 {
     using P = BPass<LB>;
     const long long blocks = count * ((1ll << l1) / P::C) << l2;
-    k_rows3<LB, INV><<<(unsigned)blocks, P::THREADS, P::SMEM, s>>>(in, out, l1, l2, out_dist, tw);
-    return cudaGetLastError();
+    return launch_pdl(k_rows3<LB, INV>, dim3((unsigned)blocks), dim3(P::THREADS), P::SMEM, s, in, out, l1, l2, out_dist,
+                      tw);
 }
 
 template <bool INV>
@@ -295,10 +300,10 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
     if (e != cudaSuccess) return e;
     const long long work = count * (M / 2 + 1);
     const int threads = 256;
-    k_split_inplace<<<(unsigned)((work + threads - 1) / threads), threads, 0, s>>>(
-        (float2*)out, count, lm, out_dist, tw);
+    e = launch_pdl(k_split_inplace, dim3((unsigned)((work + threads - 1) / threads)), dim3(threads), 0, s,
+                   (float2*)out, count, lm, out_dist, tw);
     count_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long count,
@@ -312,10 +317,9 @@ cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long cou
         return launch_l2pass(3, lm, in, out, count, in_dist, out_dist / 2, tw, scratch, scratch_bytes, s);
     const long long work = count * M;
     const int threads = 256;
-    k_merge<<<(unsigned)((work + threads - 1) / threads), threads, 0, s>>>(
-        (const float2*)in, (float2*)out, count, lm, in_dist, out_dist / 2, tw);
+    cudaError_t e = launch_pdl(k_merge, dim3((unsigned)((work + threads - 1) / threads)), dim3(threads), 0, s,
+                               (const float2*)in, (float2*)out, count, lm, in_dist, out_dist / 2, tw);
     count_launch();
-    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // inverse complex transform of the merged values, in place through scratch
     return launch_large_c2c(true, lm, out, out, count, out_dist / 2, out_dist / 2, tw, scratch,

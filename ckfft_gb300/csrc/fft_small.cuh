@@ -233,6 +233,7 @@ k_c2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
     using C = SmallCfg<L>;
+    pdl_start();
     extern __shared__ float2 smem[];
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
     const long long f = (long long)blockIdx.x * C::TPB + g;
@@ -245,6 +246,7 @@ k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
     using C = SmallCfg<LM>;
+    pdl_start();
     extern __shared__ float2 smem[];
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
     const long long f = (long long)blockIdx.x * C::TPB + g;
@@ -257,6 +259,7 @@ k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
     using C = SmallCfg<LM>;
+    pdl_start();
     extern __shared__ float2 smem[];
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
     const long long f = (long long)blockIdx.x * C::TPB + g;
@@ -276,9 +279,8 @@ cudaError_t launch_c2c_L(const void* in, void* out, long long count, long long i
                          long long out_dist, const float2* tw, cudaStream_t s)
 {
     using C = SmallCfg<L>;
-    k_c2c_small<L, INV><<<small_grid<C>(count), C::THREADS, C::SMEM, s>>>(
-        (const float2*)in, (float2*)out, count, in_dist, out_dist, tw);
-    return cudaGetLastError();
+    return launch_pdl(k_c2c_small<L, INV>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
+                      (const float2*)in, (float2*)out, count, in_dist, out_dist, tw);
 }
 
 template <int LM>
@@ -286,9 +288,8 @@ cudaError_t launch_r2c_L(const void* in, void* out, long long count, long long i
                          long long out_dist, const float2* tw, cudaStream_t s)
 {
     using C = SmallCfg<LM>;
-    k_r2c_small<LM><<<small_grid<C>(count), C::THREADS, C::SMEM, s>>>(
-        (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw);
-    return cudaGetLastError();
+    return launch_pdl(k_r2c_small<LM>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
+                      (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw);
 }
 
 template <int LM>
@@ -296,9 +297,8 @@ cudaError_t launch_c2r_L(const void* in, void* out, long long count, long long i
                          long long out_dist, const float2* tw, cudaStream_t s)
 {
     using C = SmallCfg<LM>;
-    k_c2r_small<LM><<<small_grid<C>(count), C::THREADS, C::SMEM, s>>>(
-        (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw);
-    return cudaGetLastError();
+    return launch_pdl(k_c2r_small<LM>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
+                      (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw);
 }
 
 template <int L, bool INV>

@@ -121,6 +121,26 @@ size_t large_scratch_bytes(Kind kind, int log2n);
 // device.  Idempotent; called when a context is created.
 cudaError_t prepare_device();
 
+// Launches `kernel` with programmatic stream serialization: it may start
+// while the previous kernel in the stream finishes; the kernel must call
+// pdl_start() (fft_core.cuh) before touching memory.
+template <class... KArgs, class... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Kernel launches issued so far by this process.
 long long launch_count();
 void count_launch(int n = 1);
