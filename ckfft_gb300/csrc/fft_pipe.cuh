@@ -49,6 +49,7 @@ k_pipe(const float2* __restrict__ in, float2* __restrict__ out, long long ngroup
     extern __shared__ __align__(128) float2 smem[];
     __shared__ __align__(8) unsigned long long bars[NBUF];
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    pdl_start();
 
     if (threadIdx.x == 0) {
         for (int b = 0; b < NBUF; ++b) mbar_init(smem_addr(&bars[b]), 1);
@@ -176,9 +177,10 @@ cudaError_t launch_pipe(const void* in, void* out, long long count, long long in
         if (ngroups < 1 || in_dist != P::FRAME_IN || ((uintptr_t)in & 15) || (P::GROUP_BYTES & 15) || !err)
             return cudaSuccess;
         const int grid = pipe_grid<L, KIND, NBUF>(ngroups);
-        k_pipe<L, KIND, NBUF><<<grid, C::THREADS, P::SMEM, s>>>((const float2*)in, (float2*)out, ngroups, out_dist, tw, err);
+        const cudaError_t e = launch_pdl(k_pipe<L, KIND, NBUF>, dim3(grid), dim3(C::THREADS), P::SMEM, s,
+                                         (const float2*)in, (float2*)out, ngroups, out_dist, tw, err);
         *done = ngroups * C::TPB;
-        return cudaGetLastError();
+        return e;
     }
 }
 
