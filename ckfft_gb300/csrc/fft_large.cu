@@ -89,6 +89,22 @@ k_rows3(const float2* __restrict__ in, float2* __restrict__ out, int l1, int l2,
         in + f * n + (k2 << LB), out + f * out_dist + (k2 << l1), l1 + l2, tile, threadIdx.x, smem, tw, true, l2 + LB);
 }
 
+// Row pass of a real forward transform with the split fused: block
+// (f, tile) writes the M+1 output bins of its row pairs (pass_rows_split).
+template <int LB>
+__global__ void __launch_bounds__(BPass<LB>::THREADS)
+k_rows_split(const float2* __restrict__ in, float2* __restrict__ out, int log2n1, long long in_dist,
+             long long out_dist, const float2* __restrict__ tw)
+{
+    using P = BPass<LB>;
+    extern __shared__ float2 smem[];
+    pdl_start();
+    const long long tiles = (1ll << log2n1) / P::C;
+    const long long f = blockIdx.x / tiles;
+    pass_rows_split<LB, BatchMaxT<LB>::value>(in + f * in_dist, out + f * out_dist, log2n1, blockIdx.x % tiles,
+                                              threadIdx.x, smem, tw);
+}
+
 // ------------------------------------------------- real split / merge passes
 
 // In-place split of a natural-order half-length spectrum Z (M = 2^lm values,
@@ -286,6 +302,48 @@ cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out,
     return cudaSuccess;
 }
 
+template <int LB>
+static cudaError_t launch_rows_split_L(const float2* in, float2* out, long long count, int log2n1,
+                                       long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
+{
+    using P = BPass<LB>;
+    const long long blocks = count * ((1ll << log2n1) / P::C);
+    return launch_pdl(k_rows_split<LB>, dim3((unsigned)blocks), dim3(P::THREADS), P::SMEM, s, in, out, log2n1,
+                      in_dist, out_dist, tw);
+}
+
+// Two-pass real forward with the split fused into the row pass, for half
+// lengths whose row sub-length is 2^8 .. 2^10 below the three-pass sizes.
+static bool rows_split_supported(int lm)
+{
+    const LargePlan p = large_plan(lm);
+    return lm > kSmallMaxLog2Complex && lm < kThreePassMinLog2 && p.log2n1 >= 7 && p.log2n2 >= 8 && p.log2n2 <= 10;
+}
+
+static cudaError_t launch_r2c_rows_split(int lm, const float2* in, float2* out, long long count, long long in_dist,
+                                         long long out_dist, const float2* tw, float2* tmp, size_t scratch_bytes,
+                                         cudaStream_t s)
+{
+    const LargePlan p = large_plan(lm);
+    const long long M = 1ll << lm;
+    const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)M));
+    if (group < 1) return cudaErrorInvalidValue;
+    for (long long off = 0; off < count; off += group) {
+        const long long cnt = count - off < group ? count - off : group;
+        cudaError_t e = launch_cols<false>(p.log2n1, in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s);
+        if (e != cudaSuccess) return e;
+        switch (p.log2n2) {
+        case 8: e = launch_rows_split_L<8>(tmp, out + off * out_dist, cnt, p.log2n1, M, out_dist, tw, s); break;
+        case 9: e = launch_rows_split_L<9>(tmp, out + off * out_dist, cnt, p.log2n1, M, out_dist, tw, s); break;
+        case 10: e = launch_rows_split_L<10>(tmp, out + off * out_dist, cnt, p.log2n1, M, out_dist, tw, s); break;
+        default: return cudaErrorInvalidValue;
+        }
+        if (e != cudaSuccess) return e;
+        count_launch(2);
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long count,
                              long long in_dist, long long out_dist, const float2* tw,
                              void* scratch, size_t scratch_bytes, cudaStream_t s)
@@ -295,6 +353,10 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
     const long long M = 1ll << lm;
     if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0 && scratch_bytes >= sizeof(float2) * (size_t)M)
         return launch_l2pass(2, lm, in, out, count, in_dist / 2, out_dist, tw, scratch, scratch_bytes, s);
+    if (count <= 0) return cudaSuccess;
+    if (rows_split_supported(lm) && ((uintptr_t)scratch & 127) == 0)
+        return launch_r2c_rows_split(lm, (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw,
+                                     (float2*)scratch, scratch_bytes, s);
     cudaError_t e = launch_large_c2c(false, lm, in, out, count, in_dist / 2, out_dist, tw, scratch,
                                      scratch_bytes, s);
     if (e != cudaSuccess) return e;
@@ -334,6 +396,9 @@ static cudaError_t attr_pass()
     if constexpr (L <= 10) {
         if ((e = cudaFuncSetAttribute(k_rows3<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
         if ((e = cudaFuncSetAttribute(k_rows3<L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
+    }
+    if constexpr (L >= 8 && L <= 10) {
+        if ((e = cudaFuncSetAttribute(k_rows_split<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     }
     if ((e = cudaFuncSetAttribute(k_cols<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(k_cols<L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;

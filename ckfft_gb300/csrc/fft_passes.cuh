@@ -165,6 +165,82 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
     }
 }
 
+// Row pass of a real forward transform with the split fused (half-length
+// spectrum of M = N1 N2 values, x2 scaling of the reference): tile u holds
+// rows k1 = u C/2 + j and their mirrors N1 - k1 (j < C/2; tile 0 holds row
+// N1/2 in place of the mirror of row 0), so both members of every output
+// pair (k, M - k) -- k = k1 + N1 k2, M - k = (N1 - k1) + N1 (N2 - 1 - k2) --
+// are in one CTA.  After the row DFTs the tile's half-length spectrum stays
+// in shared memory and the CTA writes the bins X[k], X[M-k] (M+1 bins per
+// transform) directly: no split pass over HBM.  Same algebra and rounding as
+// split_pair_inplace.
+template <int LB, int MAXT = 512>
+__device__ __forceinline__ void pass_rows_split(const float2* __restrict__ in, float2* __restrict__ out,
+                                                int log2n1, long long tile, int tid, float2* smem,
+                                                const float2* __restrict__ tw)
+{
+    using P = PassCfg<LB, MAXT>;
+    constexpr int N2 = 1 << LB, H = P::C / 2;
+    static_assert(P::C >= 2 && P::C % 2 == 0, "tiles of row pairs");
+    const int n1 = 1 << log2n1;
+    const long long M = (long long)n1 << LB;
+    const float2* twn = tw + 2 * M;
+    const int u = (int)tile;
+    const int r = tid / P::T, t = tid % P::T;
+    // this thread's row
+    int k1;
+    if (r < H) k1 = u * H + r;
+    else k1 = (u == 0 && r == H) ? n1 / 2 : n1 - (u * H + (r - H));
+    const float2* src = in + (long long)k1 * N2 + t;
+    float2 v[P::R];
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) v[m] = __ldcs(src + m * P::T);
+    PaddedView view{smem + r * padded_len(N2)};
+    stockham<LB, P::LOG2R, false, (P::T <= 32)>(v, t, tw, view);
+    __syncthreads();
+    {
+        // every thread has consumed its inputs: the intermediate rows are
+        // dead, so drop their L2 lines instead of writing them back
+        static_assert(N2 % 16 == 0, "rows span whole 128-byte lines");
+        const char* row = (const char*)(in + (long long)k1 * N2);
+#pragma unroll
+        for (int l = t; l < N2 / 16; l += P::T)
+            asm volatile("discard.global.L2 [%0], 128;" ::"l"(row + 128 * l) : "memory");
+    }
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) view.st(t + m * P::T, v[m]);
+    __syncthreads();
+    auto z = [&](int slot, int k2) { return smem[slot * padded_len(N2) + PaddedView::pad(k2)]; };
+    // H pairs x N2 columns, H consecutive pairs per column
+#pragma unroll
+    for (int q = 0; q < P::R / 2; ++q) {
+        const int i = tid + q * P::THREADS;
+        const int p = i % H, k2 = i / H;
+        if (u == 0 && p == 0) {
+            // row 0 pairs (k2, N2 - k2) and row N1/2 pairs (j, N2 - 1 - j)
+            if (k2 <= N2 / 2) {
+                const long long k = (long long)n1 * k2;
+                const float2 a = z(0, k2), b = z(0, (N2 - k2) & (N2 - 1));
+                out[k] = real_split(a, b, __ldg(twn + k));
+                if (k2 != N2 / 2) out[M - k] = real_split(b, a, __ldg(twn + (M - k)));
+            }
+            const int j = k2 > N2 / 2 ? k2 - N2 / 2 - 1 : (k2 == 0 ? N2 / 2 - 1 : -1);
+            if (j >= 0) {
+                const long long k = n1 / 2 + (long long)n1 * j;
+                const float2 a = z(H, j), b = z(H, N2 - 1 - j);
+                out[k] = real_split(a, b, __ldg(twn + k));
+                out[M - k] = real_split(b, a, __ldg(twn + (M - k)));
+            }
+        } else {
+            const int A = u * H + p;
+            const long long k = A + (long long)n1 * k2;
+            const float2 a = z(p, k2), b = z(H + p, N2 - 1 - k2);
+            out[k] = real_split(a, b, __ldg(twn + k));
+            out[M - k] = real_split(b, a, __ldg(twn + (M - k)));
+        }
+    }
+}
+
 // Real forward split, in place: pair k in [0, M/2] of a natural-order
 // half-length spectrum z (room for M+1 values) becomes output bins k and M-k
 // (k = 0 gives bins 0 and M; k = M/2 the middle bin).
