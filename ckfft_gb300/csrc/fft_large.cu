@@ -105,6 +105,22 @@ k_rows_split(const float2* __restrict__ in, float2* __restrict__ out, int log2n1
                                               threadIdx.x, smem, tw);
 }
 
+// Column pass of a real inverse transform with the merge fused: block
+// (f, tile) reads the M+1 bins of its column pairs (pass_cols_merge).
+template <int LA>
+__global__ void __launch_bounds__(BPass<LA>::THREADS)
+k_cols_merge(const float2* __restrict__ in, float2* __restrict__ out, int log2n2, long long in_dist,
+             long long out_dist, const float2* __restrict__ tw)
+{
+    using P = BPass<LA>;
+    extern __shared__ float2 smem[];
+    pdl_start();
+    const long long tiles = (1ll << log2n2) / P::C;
+    const long long f = blockIdx.x / tiles;
+    pass_cols_merge<LA, BatchMaxT<LA>::value, BatchCMax<LA>::value>(in + f * in_dist, out + f * out_dist, log2n2,
+                                                                    blockIdx.x % tiles, threadIdx.x, smem, tw);
+}
+
 // ------------------------------------------------- real split / merge passes
 
 // In-place split of a natural-order half-length spectrum Z (M = 2^lm values,
@@ -368,6 +384,51 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
     return e;
 }
 
+template <int LA>
+static cudaError_t launch_cols_merge_L(const float2* in, float2* out, long long count, int log2n2,
+                                       long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
+{
+    using P = BPass<LA>;
+    const long long blocks = count * ((1ll << log2n2) / P::C);
+    return launch_pdl(k_cols_merge<LA>, dim3((unsigned)blocks), dim3(P::THREADS), P::SMEM, s, in, out, log2n2,
+                      in_dist, out_dist, tw);
+}
+
+// Two-pass real inverse with the merge fused into the column pass, for half
+// lengths whose column sub-length is 2^7 .. 2^10 below the three-pass sizes.
+static bool cols_merge_supported(int lm)
+{
+    const LargePlan p = large_plan(lm);
+    return lm > kSmallMaxLog2Complex && lm < kThreePassMinLog2 && p.log2n1 >= 7 && p.log2n1 <= 10 &&
+           p.log2n2 <= 14;
+}
+
+static cudaError_t launch_c2r_cols_merge(int lm, const float2* in, float2* out, long long count, long long in_dist,
+                                         long long out_dist, const float2* tw, float2* tmp, size_t scratch_bytes,
+                                         cudaStream_t s)
+{
+    const LargePlan p = large_plan(lm);
+    const long long M = 1ll << lm;
+    const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)M));
+    if (group < 1) return cudaErrorInvalidValue;
+    for (long long off = 0; off < count; off += group) {
+        const long long cnt = count - off < group ? count - off : group;
+        cudaError_t e;
+        switch (p.log2n1) {
+        case 7: e = launch_cols_merge_L<7>(in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s); break;
+        case 8: e = launch_cols_merge_L<8>(in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s); break;
+        case 9: e = launch_cols_merge_L<9>(in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s); break;
+        case 10: e = launch_cols_merge_L<10>(in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s); break;
+        default: return cudaErrorInvalidValue;
+        }
+        if (e != cudaSuccess) return e;
+        e = launch_rows<true>(p.log2n2, tmp, out + off * out_dist, cnt, p.log2n1, M, out_dist, tw, s);
+        if (e != cudaSuccess) return e;
+        count_launch(2);
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long count,
                              long long in_dist, long long out_dist, const float2* tw,
                              void* scratch, size_t scratch_bytes, cudaStream_t s)
@@ -377,6 +438,10 @@ cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long cou
     const long long M = 1ll << lm;
     if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0 && scratch_bytes >= sizeof(float2) * (size_t)M)
         return launch_l2pass(3, lm, in, out, count, in_dist, out_dist / 2, tw, scratch, scratch_bytes, s);
+    if (count <= 0) return cudaSuccess;
+    if (cols_merge_supported(lm) && ((uintptr_t)scratch & 127) == 0)
+        return launch_c2r_cols_merge(lm, (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw,
+                                     (float2*)scratch, scratch_bytes, s);
     const long long work = count * M;
     const int threads = 256;
     cudaError_t e = launch_pdl(k_merge, dim3((unsigned)((work + threads - 1) / threads)), dim3(threads), 0, s,
@@ -399,6 +464,9 @@ static cudaError_t attr_pass()
     }
     if constexpr (L >= 8 && L <= 10) {
         if ((e = cudaFuncSetAttribute(k_rows_split<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
+    }
+    if constexpr (L >= 7 && L <= 10) {
+        if ((e = cudaFuncSetAttribute(k_cols_merge<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     }
     if ((e = cudaFuncSetAttribute(k_cols<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(k_cols<L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;

@@ -67,25 +67,15 @@ __device__ __forceinline__ float2 big_twiddle(const float2* __restrict__ tw, int
     return INV ? conjf2(w) : w;
 }
 
-// Column pass for tile `tile` of one transform, by threads tid = 0..THREADS-1.
-// live == false: the threads take part in the barriers only (no memory
-// access outside the tile's shared memory).
-template <int LA, bool INV, bool CG, int MAXT = 512, int CMAX = 16>
-__device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
-                                          long long tile, int tid, float2* smem, const float2* __restrict__ tw,
-                                          bool live = true)
+// Tail of the column pass: v[m] = Y[k1] of column n2 at k1 = t + m T,
+// multiplied by W_N^(n2 k1) and stored at out[N2 k1 + n2].
+template <int LA, bool INV, int MAXT, int CMAX>
+__device__ __forceinline__ void cols_twiddle_store(float2 (&v)[PassCfg<LA, MAXT, CMAX>::R], float2* __restrict__ out,
+                                                   int log2n2, long long n2, int t, const float2* __restrict__ tw,
+                                                   bool live)
 {
     using P = PassCfg<LA, MAXT, CMAX>;
-    const int c = tid % P::C, t = tid / P::C;
     const long long n2len = 1ll << log2n2;
-    const long long n2 = tile * P::C + c;
-    const float2* src = in + n2;
-    float2 v[P::R];
-#pragma unroll
-    for (int m = 0; m < P::R; ++m)
-        v[m] = live ? ld_data<CG>(src + (long long)(t + m * P::T) * n2len) : make_float2(0.f, 0.f);
-    TileView<P::C> view{smem, c};
-    stockham<LA, P::LOG2R, INV, false>(v, t, tw, view);
     const int ln = LA + log2n2;
     float2* dst = out + n2 + (long long)t * n2len;
     const long long step = (long long)P::T * n2len;
@@ -114,6 +104,78 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
         __stcs(dst + (4 * q + 2) * step, cmul(v[4 * q + 2], cmul(aq, b2)));
         __stcs(dst + (4 * q + 3) * step, cmul(v[4 * q + 3], cmul(aq, b3)));
     });
+}
+
+// Column pass for tile `tile` of one transform, by threads tid = 0..THREADS-1.
+// live == false: the threads take part in the barriers only (no memory
+// access outside the tile's shared memory).
+template <int LA, bool INV, bool CG, int MAXT = 512, int CMAX = 16>
+__device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
+                                          long long tile, int tid, float2* smem, const float2* __restrict__ tw,
+                                          bool live = true)
+{
+    using P = PassCfg<LA, MAXT, CMAX>;
+    const int c = tid % P::C, t = tid / P::C;
+    const long long n2len = 1ll << log2n2;
+    const long long n2 = tile * P::C + c;
+    const float2* src = in + n2;
+    float2 v[P::R];
+#pragma unroll
+    for (int m = 0; m < P::R; ++m)
+        v[m] = live ? ld_data<CG>(src + (long long)(t + m * P::T) * n2len) : make_float2(0.f, 0.f);
+    TileView<P::C> view{smem, c};
+    stockham<LA, P::LOG2R, INV, false>(v, t, tw, view);
+    cols_twiddle_store<LA, INV, MAXT, CMAX>(v, out, log2n2, n2, t, tw, live);
+}
+
+// Column pass of a real inverse transform with the merge fused (M = N1 N2
+// complex values from the M+1 input bins X): tile u holds columns
+// n2 = u C/2 + j and their mirrors N2 - n2 (j < C/2; tile 0 holds column
+// N2/2 in place of the mirror of column 0), so for every element
+// k = N2 n1 + n2 its partner M - k = N2 (N1 - 1 - n1) + (N2 - n2) is in the
+// same tile (column 0 pairs with itself at row N1 - n1, and with X[M] at
+// row 0).  The tile's raw bins are staged in shared memory, merged there
+// (the algebra and rounding of merge_elem) and transformed: no merge pass
+// over HBM.
+template <int LA, int MAXT = 512, int CMAX = 16>
+__device__ __forceinline__ void pass_cols_merge(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
+                                                long long tile, int tid, float2* smem, const float2* __restrict__ tw)
+{
+    using P = PassCfg<LA, MAXT, CMAX>;
+    constexpr int N1 = 1 << LA, H = P::C / 2;
+    static_assert(P::C >= 2 && P::C % 2 == 0, "tiles of column pairs");
+    const int c = tid % P::C, t = tid / P::C;
+    const int n2len = 1 << log2n2;
+    const long long M = (long long)N1 << log2n2;
+    const float2* twn = tw + 2 * M;
+    const int u = (int)tile;
+    const bool edge = u == 0 && (c == 0 || c == H);      // columns 0 and N2/2 mirror themselves
+    int n2;
+    if (c < H) n2 = u * H + c;
+    else n2 = (u == 0 && c == H) ? n2len / 2 : n2len - (u * H + (c - H));
+    const int mc = edge ? c : (c < H ? c + H : c - H);    // slot of the mirror column
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) {
+        const int n1 = t + m * P::T;
+        smem[TileView<P::C>::slot(n1, c)] = __ldcs(in + (long long)n1 * n2len + n2);
+    }
+    const float2 xm = (u == 0 && c == 0 && t == 0) ? __ldcs(in + M) : make_float2(0.f, 0.f);
+    __syncthreads();
+    float2 v[P::R];
+#pragma unroll
+    for (int m = 0; m < P::R; ++m) {
+        const int n1 = t + m * P::T;
+        const long long k = (long long)n1 * n2len + n2;
+        const float2 a = smem[TileView<P::C>::slot(n1, c)];
+        float2 b;
+        if (u == 0 && c == 0) b = n1 == 0 ? xm : smem[TileView<P::C>::slot(N1 - n1, 0)];
+        else b = smem[TileView<P::C>::slot(N1 - 1 - n1, mc)];
+        v[m] = real_merge(a, b, __ldg(twn + k));
+    }
+    __syncthreads();
+    TileView<P::C> view{smem, c};
+    stockham<LA, P::LOG2R, true, false>(v, t, tw, view);
+    cols_twiddle_store<LA, true, MAXT, CMAX>(v, out, log2n2, n2, t, tw, true);
 }
 
 // Row pass for tile `tile` (rows tile*C .. tile*C+C-1) of one transform.
