@@ -38,9 +38,16 @@ struct BatchCMax {
 };
 template <int LS>
 using BPass = PassCfg<LS, BatchMaxT<LS>::value, BatchCMax<LS>::value>;
+// Resident CTAs asked of the compiler for the column kernels: at most 64
+// registers a thread, so that at sub-lengths 2^9 / 2^10 (512 threads) two
+// CTAs share an SM and one's loads overlap the other's butterflies.
+template <int LS>
+struct ColsMinBlocks {
+    static constexpr int value = 65536 / (BPass<LS>::THREADS * 64);
+};
 
 template <int LA, bool INV>
-__global__ void __launch_bounds__(BPass<LA>::THREADS)
+__global__ void __launch_bounds__(BPass<LA>::THREADS, ColsMinBlocks<LA>::value)
 k_cols(const float2* __restrict__ in, float2* __restrict__ out, long long count, int log2n2,
        long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
@@ -108,7 +115,7 @@ k_rows_split(const float2* __restrict__ in, float2* __restrict__ out, int log2n1
 // Column pass of a real inverse transform with the merge fused: block
 // (f, tile) reads the M+1 bins of its column pairs (pass_cols_merge).
 template <int LA>
-__global__ void __launch_bounds__(BPass<LA>::THREADS)
+__global__ void __launch_bounds__(BPass<LA>::THREADS, ColsMinBlocks<LA>::value)
 k_cols_merge(const float2* __restrict__ in, float2* __restrict__ out, int log2n2, long long in_dist,
              long long out_dist, const float2* __restrict__ tw)
 {
@@ -365,14 +372,16 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
                              void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
     // in: n floats per frame (n/2 packed complex), out: n/2+1 complex per frame
+    // (half lengths 2^15 / 2^16 too: the fused two-pass form measured faster
+    // than the cluster form, 2550 vs 2109 GB/s batched at n = 2^16)
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
-    if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0 && scratch_bytes >= sizeof(float2) * (size_t)M)
-        return launch_l2pass(2, lm, in, out, count, in_dist / 2, out_dist, tw, scratch, scratch_bytes, s);
     if (count <= 0) return cudaSuccess;
     if (rows_split_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_r2c_rows_split(lm, (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw,
                                      (float2*)scratch, scratch_bytes, s);
+    if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0 && scratch_bytes >= sizeof(float2) * (size_t)M)
+        return launch_l2pass(2, lm, in, out, count, in_dist / 2, out_dist, tw, scratch, scratch_bytes, s);
     cudaError_t e = launch_large_c2c(false, lm, in, out, count, in_dist / 2, out_dist, tw, scratch,
                                      scratch_bytes, s);
     if (e != cudaSuccess) return e;
