@@ -100,7 +100,7 @@ k_rows3(const float2* __restrict__ in, float2* __restrict__ out, int l1, int l2,
 // (f, tile) writes the M+1 output bins of its row pairs (pass_rows_split).
 template <int LB>
 __global__ void __launch_bounds__(BPass<LB>::THREADS)
-k_rows_split(const float2* __restrict__ in, float2* __restrict__ out, int log2n1, long long in_dist,
+k_rows_split(const float2* __restrict__ in, float2* __restrict__ out, int log2n1, int log2k1, long long in_dist,
              long long out_dist, const float2* __restrict__ tw)
 {
     using P = BPass<LB>;
@@ -109,7 +109,7 @@ k_rows_split(const float2* __restrict__ in, float2* __restrict__ out, int log2n1
     const long long tiles = (1ll << log2n1) / P::C;
     const long long f = blockIdx.x / tiles;
     pass_rows_split<LB, BatchMaxT<LB>::value>(in + f * in_dist, out + f * out_dist, log2n1, blockIdx.x % tiles,
-                                              threadIdx.x, smem, tw);
+                                              threadIdx.x, smem, tw, log2k1);
 }
 
 // Column pass of a real inverse transform with the merge fused: block
@@ -243,26 +243,41 @@ static bool plan3(int log2n, int* l1, int* l2, int* l3)
 // sub-lengths above 2^10, whose tiles are 4 or 8 wide.
 constexpr int kThreePassMinLog2 = 21;
 
-static cudaError_t launch_three_pass(bool inverse, int log2n, const float2* in, float2* out, long long count,
+static cudaError_t launch_rows_split(int lb, const float2* in, float2* out, long long count, int log2n1, int log2k1,
+                                     long long in_dist, long long out_dist, const float2* tw, cudaStream_t s);
+static cudaError_t launch_cols_merge(int la, const float2* in, float2* out, long long count, int log2n2,
+                                     long long in_dist, long long out_dist, const float2* tw, cudaStream_t s);
+
+// kind C2C_FWD / C2C_INV: complex transforms of 2^log2n points.  R2C: real
+// forward of 2^(log2n+1) reals read as 2^log2n packed pairs, the split fused
+// into the third pass (2^log2n + 1 bins out).  C2R: real inverse from
+// 2^log2n + 1 bins, the merge fused into the first pass.  Distances in float2.
+static cudaError_t launch_three_pass(Kind kind, int log2n, const float2* in, float2* out, long long count,
                                      long long in_dist, long long out_dist, const float2* tw, float2* tmp,
                                      long long group, cudaStream_t s)
 {
     int l1, l2, l3;
     if (!plan3(log2n, &l1, &l2, &l3)) return cudaErrorInvalidValue;
+    const bool inverse = kind == C2C_INV || kind == C2R;
     const long long n = 1ll << log2n, M = 1ll << (l2 + l3);
     for (long long off = 0; off < count; off += group) {
         const long long cnt = count - off < group ? count - off : group;
+        const float2* src = in + off * in_dist;
+        float2* dst = out + off * out_dist;
         // pass 1: columns of length N1 over the M = N2 N3 columns -> tmp
-        cudaError_t e = inverse ? launch_cols<true>(l1, in + off * in_dist, tmp, cnt, l2 + l3, in_dist, n, tw, s)
-                                : launch_cols<false>(l1, in + off * in_dist, tmp, cnt, l2 + l3, in_dist, n, tw, s);
+        cudaError_t e = kind == C2R       ? launch_cols_merge(l1, src, tmp, cnt, l2 + l3, in_dist, n, tw, s)
+                        : inverse         ? launch_cols<true>(l1, src, tmp, cnt, l2 + l3, in_dist, n, tw, s)
+                                          : launch_cols<false>(l1, src, tmp, cnt, l2 + l3, in_dist, n, tw, s);
         // pass 2: in every row k1, columns of length N2 over the N3 columns, in place
         if (e == cudaSuccess)
             e = inverse ? launch_cols<true>(l2, tmp, tmp, cnt << l1, l3, M, M, tw, s)
                         : launch_cols<false>(l2, tmp, tmp, cnt << l1, l3, M, M, tw, s);
-        // pass 3: rows of length N3, C consecutive k1 per tile -> out
+        // pass 3: rows of length N3, C consecutive k1 per tile -> out (real
+        // forward: row pairs k, N1 N2 - k with the split)
         if (e == cudaSuccess)
-            e = inverse ? launch_rows3<true>(l3, tmp, out + off * out_dist, cnt, l1, l2, out_dist, tw, s)
-                        : launch_rows3<false>(l3, tmp, out + off * out_dist, cnt, l1, l2, out_dist, tw, s);
+            e = kind == R2C ? launch_rows_split(l3, tmp, dst, cnt, l1 + l2, l1, n, out_dist, tw, s)
+                : inverse   ? launch_rows3<true>(l3, tmp, dst, cnt, l1, l2, out_dist, tw, s)
+                            : launch_rows3<false>(l3, tmp, dst, cnt, l1, l2, out_dist, tw, s);
         if (e != cudaSuccess) return e;
         count_launch(3);
     }
@@ -309,7 +324,8 @@ cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out,
     float2* dst = (float2*)out;
     float2* tmp = (float2*)scratch;
     if (log2n >= kThreePassMinLog2 && ((uintptr_t)scratch & 127) == 0)
-        return launch_three_pass(inverse, log2n, src, dst, count, in_dist, out_dist, tw, tmp, group, s);
+        return launch_three_pass(inverse ? C2C_INV : C2C_FWD, log2n, src, dst, count, in_dist, out_dist, tw, tmp,
+                                 group, s);
     for (long long off = 0; off < count; off += group) {
         const long long cnt = count - off < group ? count - off : group;
         cudaError_t e = inverse
@@ -326,13 +342,26 @@ cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out,
 }
 
 template <int LB>
-static cudaError_t launch_rows_split_L(const float2* in, float2* out, long long count, int log2n1,
+static cudaError_t launch_rows_split_L(const float2* in, float2* out, long long count, int log2n1, int log2k1,
                                        long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
 {
     using P = BPass<LB>;
     const long long blocks = count * ((1ll << log2n1) / P::C);
     return launch_pdl(k_rows_split<LB>, dim3((unsigned)blocks), dim3(P::THREADS), P::SMEM, s, in, out, log2n1,
-                      in_dist, out_dist, tw);
+                      log2k1, in_dist, out_dist, tw);
+}
+
+// Row pass with the real split fused, row sub-length 2^lb (7 .. 10).
+static cudaError_t launch_rows_split(int lb, const float2* in, float2* out, long long count, int log2n1, int log2k1,
+                                     long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
+{
+    switch (lb) {
+    case 7: return launch_rows_split_L<7>(in, out, count, log2n1, log2k1, in_dist, out_dist, tw, s);
+    case 8: return launch_rows_split_L<8>(in, out, count, log2n1, log2k1, in_dist, out_dist, tw, s);
+    case 9: return launch_rows_split_L<9>(in, out, count, log2n1, log2k1, in_dist, out_dist, tw, s);
+    case 10: return launch_rows_split_L<10>(in, out, count, log2n1, log2k1, in_dist, out_dist, tw, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 // Two-pass real forward with the split fused into the row pass, for half
@@ -354,13 +383,8 @@ static cudaError_t launch_r2c_rows_split(int lm, const float2* in, float2* out, 
     for (long long off = 0; off < count; off += group) {
         const long long cnt = count - off < group ? count - off : group;
         cudaError_t e = launch_cols<false>(p.log2n1, in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s);
-        if (e != cudaSuccess) return e;
-        switch (p.log2n2) {
-        case 8: e = launch_rows_split_L<8>(tmp, out + off * out_dist, cnt, p.log2n1, M, out_dist, tw, s); break;
-        case 9: e = launch_rows_split_L<9>(tmp, out + off * out_dist, cnt, p.log2n1, M, out_dist, tw, s); break;
-        case 10: e = launch_rows_split_L<10>(tmp, out + off * out_dist, cnt, p.log2n1, M, out_dist, tw, s); break;
-        default: return cudaErrorInvalidValue;
-        }
+        if (e == cudaSuccess)
+            e = launch_rows_split(p.log2n2, tmp, out + off * out_dist, cnt, p.log2n1, p.log2n1, M, out_dist, tw, s);
         if (e != cudaSuccess) return e;
         count_launch(2);
     }
@@ -382,6 +406,13 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
                                      (float2*)scratch, scratch_bytes, s);
     if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0 && scratch_bytes >= sizeof(float2) * (size_t)M)
         return launch_l2pass(2, lm, in, out, count, in_dist / 2, out_dist, tw, scratch, scratch_bytes, s);
+    int l1, l2, l3;
+    if (lm >= kThreePassMinLog2 && plan3(lm, &l1, &l2, &l3) && ((uintptr_t)scratch & 127) == 0) {
+        const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)M));
+        if (group < 1) return cudaErrorInvalidValue;
+        return launch_three_pass(R2C, lm, (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw,
+                                 (float2*)scratch, group, s);
+    }
     cudaError_t e = launch_large_c2c(false, lm, in, out, count, in_dist / 2, out_dist, tw, scratch,
                                      scratch_bytes, s);
     if (e != cudaSuccess) return e;
@@ -403,6 +434,19 @@ static cudaError_t launch_cols_merge_L(const float2* in, float2* out, long long 
                       in_dist, out_dist, tw);
 }
 
+// Column pass with the real merge fused, column sub-length 2^la (7 .. 10).
+static cudaError_t launch_cols_merge(int la, const float2* in, float2* out, long long count, int log2n2,
+                                     long long in_dist, long long out_dist, const float2* tw, cudaStream_t s)
+{
+    switch (la) {
+    case 7: return launch_cols_merge_L<7>(in, out, count, log2n2, in_dist, out_dist, tw, s);
+    case 8: return launch_cols_merge_L<8>(in, out, count, log2n2, in_dist, out_dist, tw, s);
+    case 9: return launch_cols_merge_L<9>(in, out, count, log2n2, in_dist, out_dist, tw, s);
+    case 10: return launch_cols_merge_L<10>(in, out, count, log2n2, in_dist, out_dist, tw, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 // Two-pass real inverse with the merge fused into the column pass, for half
 // lengths whose column sub-length is 2^7 .. 2^10 below the three-pass sizes.
 static bool cols_merge_supported(int lm)
@@ -422,14 +466,7 @@ static cudaError_t launch_c2r_cols_merge(int lm, const float2* in, float2* out, 
     if (group < 1) return cudaErrorInvalidValue;
     for (long long off = 0; off < count; off += group) {
         const long long cnt = count - off < group ? count - off : group;
-        cudaError_t e;
-        switch (p.log2n1) {
-        case 7: e = launch_cols_merge_L<7>(in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s); break;
-        case 8: e = launch_cols_merge_L<8>(in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s); break;
-        case 9: e = launch_cols_merge_L<9>(in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s); break;
-        case 10: e = launch_cols_merge_L<10>(in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s); break;
-        default: return cudaErrorInvalidValue;
-        }
+        cudaError_t e = launch_cols_merge(p.log2n1, in + off * in_dist, tmp, cnt, p.log2n2, in_dist, M, tw, s);
         if (e != cudaSuccess) return e;
         e = launch_rows<true>(p.log2n2, tmp, out + off * out_dist, cnt, p.log2n1, M, out_dist, tw, s);
         if (e != cudaSuccess) return e;
@@ -451,6 +488,13 @@ cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long cou
     if (cols_merge_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_c2r_cols_merge(lm, (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw,
                                      (float2*)scratch, scratch_bytes, s);
+    int l1, l2, l3;
+    if (lm >= kThreePassMinLog2 && plan3(lm, &l1, &l2, &l3) && ((uintptr_t)scratch & 127) == 0) {
+        const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)M));
+        if (group < 1) return cudaErrorInvalidValue;
+        return launch_three_pass(C2R, lm, (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw,
+                                 (float2*)scratch, group, s);
+    }
     const long long work = count * M;
     const int threads = 256;
     cudaError_t e = launch_pdl(k_merge, dim3((unsigned)((work + threads - 1) / threads)), dim3(threads), 0, s,
@@ -471,7 +515,7 @@ static cudaError_t attr_pass()
         if ((e = cudaFuncSetAttribute(k_rows3<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
         if ((e = cudaFuncSetAttribute(k_rows3<L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     }
-    if constexpr (L >= 8 && L <= 10) {
+    if constexpr (L >= 7 && L <= 10) {
         if ((e = cudaFuncSetAttribute(k_rows_split<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     }
     if constexpr (L >= 7 && L <= 10) {

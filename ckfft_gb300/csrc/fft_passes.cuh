@@ -236,10 +236,14 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
 // in shared memory and the CTA writes the bins X[k], X[M-k] (M+1 bins per
 // transform) directly: no split pass over HBM.  Same algebra and rounding as
 // split_pair_inplace.
+// The third pass of the three-pass transform is the same pass over
+// N1 = N1' N2' rows: row k1' + N1' k2' sits at in[k1' N2' N3 + k2' N3] (the
+// intermediate of the second pass); log2k1 = log2 N1' selects that address
+// form (log2k1 = log2n1: rows back to back).
 template <int LB, int MAXT = 512>
 __device__ __forceinline__ void pass_rows_split(const float2* __restrict__ in, float2* __restrict__ out,
                                                 int log2n1, long long tile, int tid, float2* smem,
-                                                const float2* __restrict__ tw)
+                                                const float2* __restrict__ tw, int log2k1)
 {
     using P = PassCfg<LB, MAXT>;
     constexpr int N2 = 1 << LB, H = P::C / 2;
@@ -253,10 +257,11 @@ __device__ __forceinline__ void pass_rows_split(const float2* __restrict__ in, f
     int k1;
     if (r < H) k1 = u * H + r;
     else k1 = (u == 0 && r == H) ? n1 / 2 : n1 - (u * H + (r - H));
-    const float2* src = in + (long long)k1 * N2 + t;
+    const float2* rowp = in + ((long long)(k1 & ((1 << log2k1) - 1)) << (log2n1 - log2k1 + LB)) +
+                         ((long long)(k1 >> log2k1) << LB);
     float2 v[P::R];
 #pragma unroll
-    for (int m = 0; m < P::R; ++m) v[m] = __ldcs(src + m * P::T);
+    for (int m = 0; m < P::R; ++m) v[m] = __ldcs(rowp + t + m * P::T);
     PaddedView view{smem + r * padded_len(N2)};
     stockham<LB, P::LOG2R, false, (P::T <= 32)>(v, t, tw, view);
     __syncthreads();
@@ -264,7 +269,7 @@ __device__ __forceinline__ void pass_rows_split(const float2* __restrict__ in, f
         // every thread has consumed its inputs: the intermediate rows are
         // dead, so drop their L2 lines instead of writing them back
         static_assert(N2 % 16 == 0, "rows span whole 128-byte lines");
-        const char* row = (const char*)(in + (long long)k1 * N2);
+        const char* row = (const char*)rowp;
 #pragma unroll
         for (int l = t; l < N2 / 16; l += P::T)
             asm volatile("discard.global.L2 [%0], 128;" ::"l"(row + 128 * l) : "memory");
