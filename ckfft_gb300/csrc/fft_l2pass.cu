@@ -1,5 +1,5 @@
-// fft_l2pass.cu -- complex 2^15 and 2^16 (and real 2^16, 2^17) in two
-// passes whose intermediate never reaches HBM.
+// fft_l2pass.cu -- complex 2^15 and 2^16 (and real inverse 2^16, 2^17) in
+// two passes whose intermediate never reaches HBM.
 //
 // The multi-pass transform of fft_large.cu (columns, then rows, see
 // fft_passes.cuh) runs here inside one thread-block cluster of K CTAs per
@@ -13,10 +13,9 @@
 // on GB300 (batches of 1 GiB): 2^15 3328 vs 3145 GB/s, 2^16 3439 vs 3105;
 // the kernel is then bound by the two passes' instructions, not by HBM (40 %
 // DRAM throughput, no intermediate bytes in DRAM).  At 2^17 it was slower
-// (2779 vs 2857) and is not used there.  Real 2^16 / 2^17 run the split or
-// merge as a third phase of the same cluster: forward 2090 / 2183 vs 2055 /
-// 2037 GB/s with a separate split kernel, inverse 2355 / 2444 vs 1878 / 1835
-// with a separate merge kernel.
+// (2779 vs 2857) and is not used there.  Real inverse 2^16 / 2^17 runs the
+// merge as a first phase of the same cluster: 2381 / 2456 GB/s, against
+// 2206 / 2089 with the merge fused into the batched column pass.
 #include <cooperative_groups.h>
 
 #include "fft_passes.cuh"
@@ -55,38 +54,6 @@ __device__ __forceinline__ void cluster_barrier(cg::cluster_group& cluster)
     cluster.sync();
 }
 
-// The real forward split of a whole half-length spectrum y (n values, room
-// for n+1) by the cluster's CT threads, idx = this thread's rank: pair k
-// (k = 0 .. n/2) gives bins k and n-k, the algebra of split_pair_inplace.
-// Each thread first loads a batch of its pairs (they come from L2), then
-// computes and stores them, so the loads are in flight together.
-template <long long N, int CT>
-__device__ __forceinline__ void split_phase(float2* __restrict__ y, int idx, const float2* __restrict__ twn)
-{
-    constexpr int PER = (int)((N / 2 + CT) / CT);
-    constexpr int B = 8;
-#pragma unroll 1
-    for (int j0 = 0; j0 < PER; j0 += B) {
-        float2 a[B], b[B];
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            const long long k = idx + (long long)(j0 + j) * CT;
-            if (j0 + j < PER && k <= N / 2) {
-                a[j] = __ldcg(y + k);
-                b[j] = __ldcg(y + ((N - k) & (N - 1)));
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            const long long k = idx + (long long)(j0 + j) * CT;
-            if (j0 + j < PER && k <= N / 2) {
-                y[k] = real_split(a[j], b[j], __ldg(twn + k));
-                if (k != N / 2) y[N - k] = real_split(b[j], a[j], __ldg(twn + (N - k)));
-            }
-        }
-    }
-}
-
 // The real inverse merge of n+1 bins x into n values s (merge_elem's algebra).
 template <long long N, int CT>
 __device__ __forceinline__ void merge_phase(const float2* __restrict__ x, float2* __restrict__ s, int idx,
@@ -114,11 +81,10 @@ __device__ __forceinline__ void merge_phase(const float2* __restrict__ x, float2
 // One transform per cluster: blockIdx.x / K.  scratch holds 2^(LA+LB) values
 // per transform of the launch (128-byte aligned rows).
 // KIND 0 / 1: complex forward / inverse of n = 2^(LA+LB) points.
-// KIND 2: real forward of 2n reals (read as n packed pairs; in_dist in pairs):
-//         the complex forward, then the split of the half-length spectrum in
-//         place on the output (n+1 bins), a third phase inside the cluster.
 // KIND 3: real inverse to 2n reals (out_dist in pairs): the merge of the n+1
 //         bins into the intermediate first, then the complex inverse.
+// (Real forward runs as two batched passes with the split fused into the
+// row pass, which measured faster than a split phase here.)
 template <int LA, int LB, int KIND>
 __global__ void __cluster_dims__(kL2Cluster, 1, 1) __launch_bounds__(kL2Threads, 4)
 k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __restrict__ scratch, long long in_dist,
@@ -136,7 +102,7 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     const float2* x = in + f * in_dist;
     float2* y = out + f * out_dist;
     float2* s = scratch + f * n;
-    const float2* twn = tw + 2 * n;                  // W_(2n): split / merge twiddles
+    const float2* twn = tw + 2 * n;                  // W_(2n): merge twiddles
 
     if constexpr (KIND == 3) {
         merge_phase<n, CT>(x, s, rank * kL2Threads + threadIdx.x, twn);
@@ -157,15 +123,8 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
 #pragma unroll 1
     for (int i = 0; i < C::ITER_B; ++i) {
         const int tile = (i * kL2Cluster + rank) * C::SGB + sgb;
-        pass_rows<LB, INV, true, kL2Threads, true, KIND != 2>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, tw);
+        pass_rows<LB, INV, true, kL2Threads, true, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, tw);
         __syncthreads();
-    }
-    if constexpr (KIND == 2) {
-        // split in place: the half-length spectrum was just written (in L2)
-        cluster_barrier(cluster);
-        split_phase<n, CT>(y, rank * kL2Threads + threadIdx.x, twn);
-        // peers of this CTA may still read the lines it wrote; nothing else
-        // is shared, so the CTAs may leave independently
     }
 }
 
@@ -180,12 +139,12 @@ static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, l
 
 bool l2pass_supported(int log2n) { return log2n >= 15 && log2n <= 16; }
 
-// kind: 0 / 1 complex forward / inverse, 2 / 3 real forward / inverse whose
-// half length is 2^log2n (dists in complex units / packed pairs).
+// kind: 0 / 1 complex forward / inverse, 3 real inverse whose half length is
+// 2^log2n (dists in complex units / packed pairs).
 cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,
                           long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
-    if (!l2pass_supported(log2n) || kind < 0 || kind > 3) return cudaErrorInvalidValue;
+    if (!l2pass_supported(log2n) || (kind != 0 && kind != 1 && kind != 3)) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;
     const long long n = 1ll << log2n;
     const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
@@ -202,7 +161,6 @@ cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long l
     switch (kind) {                                                                                \
     case 0: e = launch_l2_L<LA, LB, 0>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
     case 1: e = launch_l2_L<LA, LB, 1>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
-    case 2: e = launch_l2_L<LA, LB, 2>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
     default: e = launch_l2_L<LA, LB, 3>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;          \
     }
         if (log2n == 15) { CKG_L2_KIND(7, 8) }
@@ -221,7 +179,6 @@ static cudaError_t attr_l2()
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 0>, a, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 1>, a, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 2>, a, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 3>, a, smem);
     return e;
 }

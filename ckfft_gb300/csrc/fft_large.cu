@@ -397,15 +397,14 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
 {
     // in: n floats per frame (n/2 packed complex), out: n/2+1 complex per frame
     // (half lengths 2^15 / 2^16 too: the fused two-pass form measured faster
-    // than the cluster form, 2550 vs 2109 GB/s batched at n = 2^16)
+    // than a cluster kernel with the intermediate in L2 and a split phase,
+    // 2550 vs 2109 GB/s batched at n = 2^16)
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
     if (count <= 0) return cudaSuccess;
     if (rows_split_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_r2c_rows_split(lm, (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw,
                                      (float2*)scratch, scratch_bytes, s);
-    if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0 && scratch_bytes >= sizeof(float2) * (size_t)M)
-        return launch_l2pass(2, lm, in, out, count, in_dist / 2, out_dist, tw, scratch, scratch_bytes, s);
     int l1, l2, l3;
     if (lm >= kThreePassMinLog2 && plan3(lm, &l1, &l2, &l3) && ((uintptr_t)scratch & 127) == 0) {
         const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)M));
