@@ -6,7 +6,7 @@
 // unit's operation and size:
 //   * single-CTA units run the same frame bodies as the batched kernels
 //     (fft_small.cuh), each group of T threads on its own frame pointer;
-//   * column / row / split / merge units run the multi-pass bodies
+//   * column / row units (real: merge / split fused) run the multi-pass bodies
 //     (fft_passes.cuh) with L2-only loads, because their inputs were written
 //     by other CTAs earlier in this launch (L1 is not coherent across SMs).
 // A phase unit first waits (bounded, thread 0, acquire load) for its
@@ -115,21 +115,10 @@ __device__ __noinline__ void run_pass(const UnitRec& r, const JobsArgs& a, float
     if constexpr (OP == U_COLS_FWD) pass_cols<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
     else if constexpr (OP == U_COLS_INV) pass_cols<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
     else if constexpr (OP == U_ROWS_FWD) pass_rows<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
-    else pass_rows<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
-}
-
-__device__ __noinline__ void run_split_merge(const UnitRec& r, const JobsArgs& a)
-{
-    const Unit& u = r.u;
-    const LargeDesc d = r.big;
-    const long long M = 1ll << u.log2a;
-    const float2* twn = a.tw + 2 * M;
-    const float2* src = pick(d, u.sel & 15);
-    float2* dst = pick(d, u.sel >> 4);
-    for (long long e = u.first + (long long)threadIdx.x; e < (long long)u.first + u.count; e += kJobThreads) {
-        if (u.op == U_SPLIT) split_pair_inplace<true>(dst, M, e, twn);
-        else merge_elem<true>(src, dst, M, e, twn);
-    }
+    else if constexpr (OP == U_ROWS_INV) pass_rows<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_COLS_MERGE)
+        pass_cols_merge<LS, kJobThreads, 16, true>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else pass_rows_split<LS, kJobThreads, true>(src, dst, u.log2b, tile, tid, my, a.tw, u.log2b);
 }
 
 // ---------------------------------------------------------------- dispatch
@@ -189,8 +178,8 @@ __device__ __forceinline__ void dispatch(const UnitRec& r, const JobsArgs& a, fl
     case U_COLS_INV: pass_switch<U_COLS_INV>(r, a, smem); break;
     case U_ROWS_FWD: pass_switch<U_ROWS_FWD>(r, a, smem); break;
     case U_ROWS_INV: pass_switch<U_ROWS_INV>(r, a, smem); break;
-    case U_SPLIT:
-    case U_MERGE: run_split_merge(r, a); break;
+    case U_COLS_MERGE: pass_switch<U_COLS_MERGE>(r, a, smem); break;
+    case U_ROWS_SPLIT: pass_switch<U_ROWS_SPLIT>(r, a, smem); break;
     default: break;
     }
 }

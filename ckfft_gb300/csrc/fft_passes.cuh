@@ -134,10 +134,10 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
 // N2/2 in place of the mirror of column 0), so for every element
 // k = N2 n1 + n2 its partner M - k = N2 (N1 - 1 - n1) + (N2 - n2) is in the
 // same tile (column 0 pairs with itself at row N1 - n1, and with X[M] at
-// row 0).  The tile's raw bins are staged in shared memory, merged there
-// (the algebra and rounding of merge_elem) and transformed: no merge pass
-// over HBM.
-template <int LA, int MAXT = 512, int CMAX = 16>
+// row 0).  The tile's raw bins are staged in shared memory, merged there in
+// place pair by pair (the algebra and rounding of merge_elem) and
+// transformed: no merge pass over HBM.  CG: L2-only loads, as in pass_cols.
+template <int LA, int MAXT = 512, int CMAX = 16, bool CG = false>
 __device__ __forceinline__ void pass_cols_merge(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
                                                 long long tile, int tid, float2* smem, const float2* __restrict__ tw)
 {
@@ -149,29 +149,60 @@ __device__ __forceinline__ void pass_cols_merge(const float2* __restrict__ in, f
     const long long M = (long long)N1 << log2n2;
     const float2* twn = tw + 2 * M;
     const int u = (int)tile;
-    const bool edge = u == 0 && (c == 0 || c == H);      // columns 0 and N2/2 mirror themselves
-    int n2;
-    if (c < H) n2 = u * H + c;
-    else n2 = (u == 0 && c == H) ? n2len / 2 : n2len - (u * H + (c - H));
-    const int mc = edge ? c : (c < H ? c + H : c - H);    // slot of the mirror column
+    // column of tile slot `slot`
+    auto col = [&](int slot) {
+        if (slot < H) return u * H + slot;
+        return (u == 0 && slot == H) ? n2len / 2 : n2len - (u * H + (slot - H));
+    };
+    const int n2 = col(c);
 #pragma unroll
     for (int m = 0; m < P::R; ++m) {
         const int n1 = t + m * P::T;
-        smem[TileView<P::C>::slot(n1, c)] = __ldcs(in + (long long)n1 * n2len + n2);
+        smem[TileView<P::C>::slot(n1, c)] = ld_data<CG>(in + (long long)n1 * n2len + n2);
     }
-    const float2 xm = (u == 0 && c == 0 && t == 0) ? __ldcs(in + M) : make_float2(0.f, 0.f);
+    const float2 xm = (u == 0 && tid == 0) ? ld_data<CG>(in + M) : make_float2(0.f, 0.f);   // X[M]
+    __syncthreads();
+    // Merge the pairs (k, M - k) in place: H pairs per row n1, by items
+    // i = (n1, p); tile 0's p = 0 items take columns 0 and N2/2, which pair
+    // within themselves (row n1 with N1 - n1, and with X[M] at row 0; row
+    // j with N1 - 1 - j).
+    auto S = [&](int slot, int n1) -> float2& { return smem[TileView<P::C>::slot(n1, slot)]; };
+#pragma unroll 4
+    for (int q = 0; q < P::R / 2; ++q) {
+        const int i = tid + q * P::THREADS;
+        const int p = i % H, n1 = i / H;
+        if (u == 0 && p == 0) {
+            if (n1 <= N1 / 2) {
+                const long long k = (long long)n1 * n2len;
+                const float2 a = S(0, n1);
+                if (n1 == 0) {
+                    S(0, 0) = real_merge(a, xm, __ldg(twn));
+                } else if (n1 == N1 / 2) {
+                    S(0, n1) = real_merge(a, a, __ldg(twn + k));
+                } else {
+                    const float2 b = S(0, N1 - n1);
+                    S(0, n1) = real_merge(a, b, __ldg(twn + k));
+                    S(0, N1 - n1) = real_merge(b, a, __ldg(twn + (M - k)));
+                }
+            }
+            const int j = n1 > N1 / 2 ? n1 - N1 / 2 - 1 : (n1 == 0 ? N1 / 2 - 1 : -1);
+            if (j >= 0) {
+                const long long k = (long long)j * n2len + n2len / 2;
+                const float2 a = S(H, j), b = S(H, N1 - 1 - j);
+                S(H, j) = real_merge(a, b, __ldg(twn + k));
+                S(H, N1 - 1 - j) = real_merge(b, a, __ldg(twn + (M - k)));
+            }
+        } else {
+            const long long k = (long long)n1 * n2len + (u * H + p);
+            const float2 a = S(p, n1), b = S(H + p, N1 - 1 - n1);
+            S(p, n1) = real_merge(a, b, __ldg(twn + k));
+            S(H + p, N1 - 1 - n1) = real_merge(b, a, __ldg(twn + (M - k)));
+        }
+    }
     __syncthreads();
     float2 v[P::R];
 #pragma unroll
-    for (int m = 0; m < P::R; ++m) {
-        const int n1 = t + m * P::T;
-        const long long k = (long long)n1 * n2len + n2;
-        const float2 a = smem[TileView<P::C>::slot(n1, c)];
-        float2 b;
-        if (u == 0 && c == 0) b = n1 == 0 ? xm : smem[TileView<P::C>::slot(N1 - n1, 0)];
-        else b = smem[TileView<P::C>::slot(N1 - 1 - n1, mc)];
-        v[m] = real_merge(a, b, __ldg(twn + k));
-    }
+    for (int m = 0; m < P::R; ++m) v[m] = S(c, t + m * P::T);
     __syncthreads();
     TileView<P::C> view{smem, c};
     stockham<LA, P::LOG2R, true, false>(v, t, tw, view);
@@ -239,8 +270,9 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
 // The third pass of the three-pass transform is the same pass over
 // N1 = N1' N2' rows: row k1' + N1' k2' sits at in[k1' N2' N3 + k2' N3] (the
 // intermediate of the second pass); log2k1 = log2 N1' selects that address
-// form (log2k1 = log2n1: rows back to back).
-template <int LB, int MAXT = 512>
+// form (log2k1 = log2n1: rows back to back).  CG: L2-only loads, as in
+// pass_rows.
+template <int LB, int MAXT = 512, bool CG = false>
 __device__ __forceinline__ void pass_rows_split(const float2* __restrict__ in, float2* __restrict__ out,
                                                 int log2n1, long long tile, int tid, float2* smem,
                                                 const float2* __restrict__ tw, int log2k1)
@@ -261,7 +293,7 @@ __device__ __forceinline__ void pass_rows_split(const float2* __restrict__ in, f
                          ((long long)(k1 >> log2k1) << LB);
     float2 v[P::R];
 #pragma unroll
-    for (int m = 0; m < P::R; ++m) v[m] = __ldcs(rowp + t + m * P::T);
+    for (int m = 0; m < P::R; ++m) v[m] = ld_data<CG>(rowp + t + m * P::T);
     PaddedView view{smem + r * padded_len(N2)};
     stockham<LB, P::LOG2R, false, (P::T <= 32)>(v, t, tw, view);
     __syncthreads();

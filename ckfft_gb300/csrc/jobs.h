@@ -4,8 +4,9 @@
 // persistent CTAs pop with one atomic add each:
 //   * single-CTA units: up to min(256/T, 64) frames of one kind and size,
 //     each frame with its own input / output pointer (FrameDesc);
-//   * phase units of a multi-pass transform (LargeDesc): a merge range, a set
-//     of column tiles, a set of row tiles, or a split range.  A phase unit
+//   * phase units of a multi-pass transform (LargeDesc): a set of column
+//     tiles (phase 0; real inverse: with the merge fused) or of row tiles
+//     (phase 1; real forward: with the split fused).  A phase unit
 //     names how many units of its transform must have finished first; every
 //     unit of a transform adds one to that transform's counter when done.
 // Phase-p units are queued after every phase-(p-1) unit, so a CTA only ever
@@ -29,8 +30,8 @@ enum UnitOp : int {
     U_COLS_INV = 7,
     U_ROWS_FWD = 8,    // row pass, log2a = row length, log2b = log2 rows
     U_ROWS_INV = 9,
-    U_SPLIT = 10,      // real forward split in place, log2a = log2 (n/2)
-    U_MERGE = 11,      // real inverse merge, log2a = log2 (n/2)
+    U_COLS_MERGE = 10, // real inverse: merge fused into the column pass (pass_cols_merge)
+    U_ROWS_SPLIT = 11, // real forward: split fused into the row pass (pass_rows_split)
 };
 
 // Buffer selectors of a phase unit.

@@ -10,6 +10,7 @@
 #include <map>
 #include <new>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "ckfft_cuda.h"
@@ -60,7 +61,6 @@ static int single_threads(int l)
     }
 }
 
-constexpr int kElemsPerUnit = kJobThreads * 16;  // split / merge work per unit
 
 struct Built {
     std::vector<Unit> units;
@@ -150,7 +150,7 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
         return false;
     }
     std::map<std::pair<int, int>, std::vector<FrameDesc>> buckets;   // (op, log2a) -> frames
-    std::vector<std::array<std::vector<Unit>, 3>> phases;           // per multi-pass transform
+    std::vector<std::array<std::vector<Unit>, 2>> phases;           // per multi-pass transform
     for (int j = 0; j < njobs; ++j) {
         const CkFftCudaJob& J = jobs[j];
         if (!validate_job(cv, J, j)) return false;
@@ -174,7 +174,7 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
                 const int op = real ? (inverse ? U_C2R : U_R2C) : (inverse ? U_C2C_INV : U_C2C_FWD);
                 buckets[{op, lc}].push_back({in, out});
             } else {
-                // multi-pass transform: phases of column / row tiles (+ merge or split)
+                // multi-pass transform: a phase of column tiles, then one of row tiles
                 const int job = (int)b->large.size();
                 b->large.push_back({in, out, nullptr, 0});
                 phases.emplace_back();
@@ -190,30 +190,18 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
                     for (int t = 0; t < tiles; t += per, ++added)
                         phase[p].push_back({op, ls, other, job, done, t, per, src | (dst << 4)});
                 };
-                auto add_elems = [&](int op, long long count, int src, int dst) {
-                    for (long long e = 0; e < count; e += kElemsPerUnit, ++added)
-                        phase[p].push_back({op, lc, 0, job, done, (int)e, (int)std::min<long long>(kElemsPerUnit, count - e), src | (dst << 4)});
-                };
                 auto end_phase = [&]() {
                     done += added;
                     added = 0;
                     ++p;
                 };
-                if (real && inverse) {
-                    add_elems(U_MERGE, 1ll << lc, B_IN, B_OUT);
-                    end_phase();
-                    add_pass(U_COLS_INV, la, lb, tiles_a, sa, B_OUT, B_SCRATCH);
-                    end_phase();
-                    add_pass(U_ROWS_INV, lb, la, tiles_b, sb, B_SCRATCH, B_OUT);
-                } else {
-                    add_pass(inverse ? U_COLS_INV : U_COLS_FWD, la, lb, tiles_a, sa, B_IN, B_SCRATCH);
-                    end_phase();
-                    add_pass(inverse ? U_ROWS_INV : U_ROWS_FWD, lb, la, tiles_b, sb, B_SCRATCH, B_OUT);
-                    if (real) {
-                        end_phase();
-                        add_elems(U_SPLIT, (1ll << lc) / 2 + 1, B_OUT, B_OUT);
-                    }
-                }
+                // real: the merge fused into the column pass (inverse), the
+                // split into the row pass (forward) -- two phases, like complex
+                add_pass(real && inverse ? U_COLS_MERGE : inverse ? U_COLS_INV : U_COLS_FWD, la, lb, tiles_a, sa,
+                         B_IN, B_SCRATCH);
+                end_phase();
+                add_pass(real && !inverse ? U_ROWS_SPLIT : inverse ? U_ROWS_INV : U_ROWS_FWD, lb, la, tiles_b, sb,
+                         B_SCRATCH, B_OUT);
             }
         }
     }
@@ -234,9 +222,10 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
         }
     }
     // Queue order.  The first phase of the multi-pass transforms is spread
-    // over the single-CTA units; each later phase of a transform is placed
-    // `window` units after the last unit of its previous phase.  The window
-    // (twice the resident CTAs) is long enough that the previous phase has
+    // over the single-CTA units (both grouped by type, see below); each
+    // later phase of a transform is placed `window` units after the last unit
+    // of its previous phase.  The window (twice the resident CTAs) is long
+    // enough that the previous phase has
     // usually finished when the next one is taken (no idle wait), and short
     // enough that the intermediate it wrote is still in L2.  Phase p of a
     // transform always follows all of its phase p-1, so every wait is for
@@ -249,7 +238,7 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
     std::vector<Pending> pending;       // kept sorted by `ready`
     auto push_phase = [&](int job, int p) {
         b->units.insert(b->units.end(), phases[job][p].begin(), phases[job][p].end());
-        if (p + 1 < 3 && !phases[job][p + 1].empty()) {
+        if (p + 1 < 2 && !phases[job][p + 1].empty()) {
             Pending q{b->units.size() + window, job, p + 1};
             auto it = std::upper_bound(pending.begin(), pending.end(), q,
                                        [](const Pending& x, const Pending& y) { return x.ready < y.ready; });
@@ -264,11 +253,24 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
         }
     };
     const size_t nl = phases.size();
+    // Multi-pass transforms grouped by unit type (operation, sub-lengths):
+    // the kernel holds a device function per operation and size, and a
+    // queue that mixes every type at once spills the SMs' instruction cache
+    // (the 10000-job run of log2 n 6..16: 24 M instruction-cache misses and
+    // 818 us unsorted, 2387-2399 GB/s sorted against 2016).
+    std::vector<int> jorder(nl);
+    for (size_t j = 0; j < nl; ++j) jorder[j] = (int)j;
+    auto jkey = [&](int j) {
+        const Unit& u0 = phases[j][0].front();
+        const Unit& u1 = phases[j][1].empty() ? u0 : phases[j][1].front();
+        return std::make_tuple(u0.op, u0.log2a, u1.op, u1.log2a);
+    };
+    std::stable_sort(jorder.begin(), jorder.end(), [&](int x, int y) { return jkey(x) < jkey(y); });
     size_t si = 0;
-    for (size_t j = 0; j < nl; ++j) {
-        push_phase((int)j, 0);
+    for (size_t jj = 0; jj < nl; ++jj) {
+        push_phase(jorder[jj], 0);
         drain_ready();
-        const size_t upto = singles.size() * (j + 1) / nl;
+        const size_t upto = singles.size() * (jj + 1) / nl;
         for (; si < upto; ++si) {
             b->units.push_back(singles[si]);
             drain_ready();

@@ -196,7 +196,7 @@ def test_large_complex_vs_oracle_and_fp64(torch_cuda, ctx_cache, oracle_mod, l2)
 @pytest.mark.parametrize("kind,l2,count", [("cfwd", 21, 3), ("cinv", 22, 2), ("rfwd", 22, 2), ("rinv", 23, 2),
                                             ("rfwd", 18, 3), ("rfwd", 20, 3), ("rfwd", 21, 2),
                                             ("rinv", 18, 3), ("rinv", 20, 3), ("rinv", 21, 2),
-                                            ("rfwd", 23, 2), ("rinv", 22, 2)])
+                                            ("rfwd", 23, 2), ("rinv", 22, 2), ("cfwd", 20, 3), ("cinv", 19, 4)])
 def test_three_pass_batches(torch_cuda, ctx_cache, oracle_mod, kind, l2, count):
     """Batches on the multi-pass paths (three passes; two passes with the
     real split fused into the row pass or the merge into the column pass):
