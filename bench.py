@@ -56,9 +56,12 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-percall", action="store_true")
     ap.add_argument("--direct-mb", type=int, default=8, help="w5: requests this large skip batching")
-    ap.add_argument("--workload", choices=["w1", "w2", "w3", "w4", "w5"], default="w2",
+    ap.add_argument("--workload", choices=["w1", "w2", "w3", "w4", "w5", "sizes"], default="w2",
                     help="w2 (default): real n=4096 x 65536 frames; w1: complex n=1024 x 4096 round trip; "
-                         "w3: large single complex transforms; w4: uneven mixed batch; w5: serving")
+                         "w3: large single complex transforms; w4: uneven mixed batch; w5: serving; "
+                         "sizes: batched GB/s per size and kind")
+    ap.add_argument("--sizes", default=",".join(str(i) for i in range(25)),
+                    help="sizes workload: comma-separated log2 n")
     return ap.parse_args()
 
 
@@ -579,6 +582,53 @@ def run_w3(args):
     ctx.close()
 
 
+def run_sizes(args):
+    """Batched throughput per size and kind: about 1 GiB of input per call
+    (CkFftCuda*Batch on device buffers, larger than L2, so no flush), the
+    calls of each (size, kind) enqueued back to back and timed with CUDA
+    events; GB/s of algorithmic bytes."""
+    import torch
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+
+    sizes = [int(v) for v in args.sizes.split(",")]
+    ctx = binding.Context(1 << max(1, max(sizes)))
+    stream = torch.cuda.Stream()
+    peak, src = measured_peaks()
+    table = {}
+    total_secs = 0.0
+    for l2 in sizes:
+        n = 1 << l2
+        row = {}
+        for kind in ("cfwd", "cinv", "rfwd", "rinv"):
+            real = kind[0] == "r"
+            in_b = 4 * n if kind == "rfwd" else 8 * (n // 2 + 1) if kind == "rinv" else 8 * n
+            out_b = 8 * (n // 2 + 1) if kind == "rfwd" else 4 * n if kind == "rinv" else 8 * n
+            count = max(1, (1 << 30) // in_b)
+            x = torch.randn(count * in_b // 4, device="cuda")
+            y = torch.empty(count * out_b // 4 + 4, device="cuda")
+
+            def step():
+                ctx.check(ctx.batch(kind, n, count, x, y, stream))
+
+            for _ in range(max(args.warmup, 3)):
+                step()
+            secs = timed_steps(torch, stream, step, args.steps)
+            total_secs += secs
+            row[kind] = round(args.steps * count * wl.algorithmic_bytes(real, n) / secs / 1e9, 1)
+            del x, y
+        table[f"2^{l2}"] = row
+    top = table[f"2^{sizes[-1]}"]["cfwd"]
+    line = base_line(args, f"batched FFT GB/s per size (value: complex forward at 2^{sizes[-1]})", top, "GB/s",
+                     total_secs, {"workload": "one batch of about 1 GiB of input per size and kind, device buffers",
+                                  "l2": "inputs larger than L2, no flush", "sizes": sizes})
+    line["table"] = table
+    line["roofline"] = {"bound": "hbm", "kernel": f"batched kernels at 2^{sizes[-1]}", "achieved": top, "peak": peak,
+                        "unit": "GB/s", "frac": round(top / peak, 4), "peak_source": src, "traffic": None}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_w4(args):
     """Workload 4: 10000 transforms of uneven sizes in one graph-captured persistent launch,
     against the plain path of one CkFft* call per transform."""
@@ -631,12 +681,14 @@ def run_w4(args):
                 ctx.real_forward(n, x, y)
             else:
                 ctx.real_inverse(n, x, y, tmp)
-    per_call()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    per_call()
-    torch.cuda.synchronize()
-    pc = time.perf_counter() - t0
+    pc = None
+    if not args.no_percall:
+        per_call()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        per_call()
+        torch.cuda.synchronize()
+        pc = time.perf_counter() - t0
     peak, src = measured_peaks()
     line = base_line(args, "uneven batch FFT GB/s (10000 transforms, log2 n 6..16, mixed kinds)", value, "GB/s", secs,
                      {"workload": "10000 transforms, log2 n uniform 6..16, 70% complex / 30% real, 50% inverse, "
@@ -646,9 +698,10 @@ def run_w4(args):
     line["roofline"] = {"bound": "hbm", "kernel": "k_jobs (persistent job kernel)", "achieved": round(value, 1),
                         "peak": peak, "unit": "GB/s", "frac": round(value / peak, 4), "peak_source": src,
                         "traffic": None, "note": "multi-pass jobs (2^14..2^16) move 2x their algorithmic bytes"}
-    line["per_call"] = {"transforms_per_s": round(len(jobs) / pc, 1), "gbs": round(plan.bytes / pc / 1e9, 2),
-                        "api": "one CkFftComplex*/CkFftReal* call per transform (device pointers, blocking)",
-                        "speedup_of_persistent": round(tps / (len(jobs) / pc), 1)}
+    if pc is not None:
+        line["per_call"] = {"transforms_per_s": round(len(jobs) / pc, 1), "gbs": round(plan.bytes / pc / 1e9, 2),
+                            "api": "one CkFftComplex*/CkFftReal* call per transform (device pointers, blocking)",
+                            "speedup_of_persistent": round(tps / (len(jobs) / pc), 1)}
     line["gpu_launches"] = launches
     print(json.dumps(line), flush=True)
     plan.close()
@@ -731,7 +784,7 @@ def run_w5(args, nreq=600):
 def main():
     args = parse_args()
     if args.workload != "w2" and args.impl == "ours":
-        {"w1": run_w1, "w3": run_w3, "w4": run_w4, "w5": run_w5}[args.workload](args)
+        {"w1": run_w1, "w3": run_w3, "w4": run_w4, "w5": run_w5, "sizes": run_sizes}[args.workload](args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
