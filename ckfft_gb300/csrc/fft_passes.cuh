@@ -165,38 +165,45 @@ __device__ __forceinline__ void pass_cols_merge(const float2* __restrict__ in, f
     // Merge the pairs (k, M - k) in place: H pairs per row n1, by items
     // i = (n1, p); tile 0's p = 0 items take columns 0 and N2/2, which pair
     // within themselves (row n1 with N1 - n1, and with X[M] at row 0; row
-    // j with N1 - 1 - j).
+    // j with N1 - 1 - j).  p = tid mod H for every item of a thread.
+    // Twiddles: W_2M^k = W_2N1^n1 * W_2M^n2 (k = N2 n1 + n2) -- a row factor
+    // from the short 2N1 level of the table and one column factor per
+    // thread -- and W_2M^(M-k) = -conj(W_2M^k).
     auto S = [&](int slot, int n1) -> float2& { return smem[TileView<P::C>::slot(n1, slot)]; };
+    const float2* twr = tw + 2 * N1;                                  // W_2N1^n1
+    const int pt = tid % H;
+    const bool edge = u == 0 && pt == 0;
+    const float2 wcol = __ldg(twn + (edge ? n2len / 2 : u * H + pt));  // column factor
 #pragma unroll 4
     for (int q = 0; q < P::R / 2; ++q) {
         const int i = tid + q * P::THREADS;
-        const int p = i % H, n1 = i / H;
-        if (u == 0 && p == 0) {
+        const int n1 = i / H;
+        if (edge) {
             if (n1 <= N1 / 2) {
-                const long long k = (long long)n1 * n2len;
+                const float2 w = __ldg(twr + n1);                     // column 0: W_2M^(N2 n1)
                 const float2 a = S(0, n1);
                 if (n1 == 0) {
-                    S(0, 0) = real_merge(a, xm, __ldg(twn));
+                    S(0, 0) = real_merge(a, xm, w);
                 } else if (n1 == N1 / 2) {
-                    S(0, n1) = real_merge(a, a, __ldg(twn + k));
+                    S(0, n1) = real_merge(a, a, w);
                 } else {
                     const float2 b = S(0, N1 - n1);
-                    S(0, n1) = real_merge(a, b, __ldg(twn + k));
-                    S(0, N1 - n1) = real_merge(b, a, __ldg(twn + (M - k)));
+                    S(0, n1) = real_merge(a, b, w);
+                    S(0, N1 - n1) = real_merge(b, a, make_float2(-w.x, w.y));
                 }
             }
             const int j = n1 > N1 / 2 ? n1 - N1 / 2 - 1 : (n1 == 0 ? N1 / 2 - 1 : -1);
             if (j >= 0) {
-                const long long k = (long long)j * n2len + n2len / 2;
+                const float2 w = cmul(__ldg(twr + j), wcol);          // column N2/2
                 const float2 a = S(H, j), b = S(H, N1 - 1 - j);
-                S(H, j) = real_merge(a, b, __ldg(twn + k));
-                S(H, N1 - 1 - j) = real_merge(b, a, __ldg(twn + (M - k)));
+                S(H, j) = real_merge(a, b, w);
+                S(H, N1 - 1 - j) = real_merge(b, a, make_float2(-w.x, w.y));
             }
         } else {
-            const long long k = (long long)n1 * n2len + (u * H + p);
-            const float2 a = S(p, n1), b = S(H + p, N1 - 1 - n1);
-            S(p, n1) = real_merge(a, b, __ldg(twn + k));
-            S(H + p, N1 - 1 - n1) = real_merge(b, a, __ldg(twn + (M - k)));
+            const float2 w = cmul(__ldg(twr + n1), wcol);
+            const float2 a = S(pt, n1), b = S(H + pt, N1 - 1 - n1);
+            S(pt, n1) = real_merge(a, b, w);
+            S(H + pt, N1 - 1 - n1) = real_merge(b, a, make_float2(-w.x, w.y));
         }
     }
     __syncthreads();
@@ -310,32 +317,41 @@ __device__ __forceinline__ void pass_rows_split(const float2* __restrict__ in, f
     for (int m = 0; m < P::R; ++m) view.st(t + m * P::T, v[m]);
     __syncthreads();
     auto z = [&](int slot, int k2) { return smem[slot * padded_len(N2) + PaddedView::pad(k2)]; };
-    // H pairs x N2 columns, H consecutive pairs per column
+    // H pairs x N2 columns, H consecutive pairs per column; p = tid mod H
+    // for every item of a thread.  Twiddles: W_2M^k = W_2N2^k2 * W_2M^A
+    // (k = A + N1 k2) -- a factor from the short 2N2 level of the table and
+    // one row factor per thread -- and W_2M^(M-k) = -conj(W_2M^k).
+    const float2* twc = tw + 2 * N2;                                  // W_2N2^k2
+    const int pt = tid % H;
+    const bool edge = u == 0 && pt == 0;
+    const float2 wrow = __ldg(twn + (edge ? n1 / 2 : u * H + pt));     // row factor
 #pragma unroll
     for (int q = 0; q < P::R / 2; ++q) {
         const int i = tid + q * P::THREADS;
-        const int p = i % H, k2 = i / H;
-        if (u == 0 && p == 0) {
+        const int k2 = i / H;
+        if (edge) {
             // row 0 pairs (k2, N2 - k2) and row N1/2 pairs (j, N2 - 1 - j)
             if (k2 <= N2 / 2) {
                 const long long k = (long long)n1 * k2;
+                const float2 w = __ldg(twc + k2);                     // row 0: W_2M^(N1 k2)
                 const float2 a = z(0, k2), b = z(0, (N2 - k2) & (N2 - 1));
-                out[k] = real_split(a, b, __ldg(twn + k));
-                if (k2 != N2 / 2) out[M - k] = real_split(b, a, __ldg(twn + (M - k)));
+                out[k] = real_split(a, b, w);
+                if (k2 != N2 / 2) out[M - k] = real_split(b, a, make_float2(-w.x, w.y));
             }
             const int j = k2 > N2 / 2 ? k2 - N2 / 2 - 1 : (k2 == 0 ? N2 / 2 - 1 : -1);
             if (j >= 0) {
                 const long long k = n1 / 2 + (long long)n1 * j;
+                const float2 w = cmul(__ldg(twc + j), wrow);          // row N1/2
                 const float2 a = z(H, j), b = z(H, N2 - 1 - j);
-                out[k] = real_split(a, b, __ldg(twn + k));
-                out[M - k] = real_split(b, a, __ldg(twn + (M - k)));
+                out[k] = real_split(a, b, w);
+                out[M - k] = real_split(b, a, make_float2(-w.x, w.y));
             }
         } else {
-            const int A = u * H + p;
-            const long long k = A + (long long)n1 * k2;
-            const float2 a = z(p, k2), b = z(H + p, N2 - 1 - k2);
-            out[k] = real_split(a, b, __ldg(twn + k));
-            out[M - k] = real_split(b, a, __ldg(twn + (M - k)));
+            const long long k = u * H + pt + (long long)n1 * k2;
+            const float2 w = cmul(__ldg(twc + k2), wrow);
+            const float2 a = z(pt, k2), b = z(H + pt, N2 - 1 - k2);
+            out[k] = real_split(a, b, w);
+            out[M - k] = real_split(b, a, make_float2(-w.x, w.y));
         }
     }
 }
