@@ -134,9 +134,9 @@ __device__ __forceinline__ void pass_cols(const float2* __restrict__ in, float2*
 // N2/2 in place of the mirror of column 0), so for every element
 // k = N2 n1 + n2 its partner M - k = N2 (N1 - 1 - n1) + (N2 - n2) is in the
 // same tile (column 0 pairs with itself at row N1 - n1, and with X[M] at
-// row 0).  The tile's raw bins are staged in shared memory, merged there in
-// place pair by pair (the algebra and rounding of merge_elem) and
-// transformed: no merge pass over HBM.  CG: L2-only loads, as in pass_cols.
+// row 0).  The tile's raw bins are staged in shared memory and merged into
+// registers (the algebra of merge_elem) before the column DFTs: no merge
+// pass over HBM.  CG: L2-only loads, as in pass_cols.
 template <int LA, int MAXT = 512, int CMAX = 16, bool CG = false>
 __device__ __forceinline__ void pass_cols_merge(const float2* __restrict__ in, float2* __restrict__ out, int log2n2,
                                                 long long tile, int tid, float2* smem, const float2* __restrict__ tw)
@@ -162,54 +162,26 @@ __device__ __forceinline__ void pass_cols_merge(const float2* __restrict__ in, f
     }
     const float2 xm = (u == 0 && tid == 0) ? ld_data<CG>(in + M) : make_float2(0.f, 0.f);   // X[M]
     __syncthreads();
-    // Merge the pairs (k, M - k) in place: H pairs per row n1, by items
-    // i = (n1, p); tile 0's p = 0 items take columns 0 and N2/2, which pair
-    // within themselves (row n1 with N1 - n1, and with X[M] at row 0; row
-    // j with N1 - 1 - j).  p = tid mod H for every item of a thread.
-    // Twiddles: W_2M^k = W_2N1^n1 * W_2M^n2 (k = N2 n1 + n2) -- a row factor
-    // from the short 2N1 level of the table and one column factor per
-    // thread -- and W_2M^(M-k) = -conj(W_2M^k).
-    auto S = [&](int slot, int n1) -> float2& { return smem[TileView<P::C>::slot(n1, slot)]; };
-    const float2* twr = tw + 2 * N1;                                  // W_2N1^n1
-    const int pt = tid % H;
-    const bool edge = u == 0 && pt == 0;
-    const float2 wcol = __ldg(twn + (edge ? n2len / 2 : u * H + pt));  // column factor
-#pragma unroll 4
-    for (int q = 0; q < P::R / 2; ++q) {
-        const int i = tid + q * P::THREADS;
-        const int n1 = i / H;
-        if (edge) {
-            if (n1 <= N1 / 2) {
-                const float2 w = __ldg(twr + n1);                     // column 0: W_2M^(N2 n1)
-                const float2 a = S(0, n1);
-                if (n1 == 0) {
-                    S(0, 0) = real_merge(a, xm, w);
-                } else if (n1 == N1 / 2) {
-                    S(0, n1) = real_merge(a, a, w);
-                } else {
-                    const float2 b = S(0, N1 - n1);
-                    S(0, n1) = real_merge(a, b, w);
-                    S(0, N1 - n1) = real_merge(b, a, make_float2(-w.x, w.y));
-                }
-            }
-            const int j = n1 > N1 / 2 ? n1 - N1 / 2 - 1 : (n1 == 0 ? N1 / 2 - 1 : -1);
-            if (j >= 0) {
-                const float2 w = cmul(__ldg(twr + j), wcol);          // column N2/2
-                const float2 a = S(H, j), b = S(H, N1 - 1 - j);
-                S(H, j) = real_merge(a, b, w);
-                S(H, N1 - 1 - j) = real_merge(b, a, make_float2(-w.x, w.y));
-            }
-        } else {
-            const float2 w = cmul(__ldg(twr + n1), wcol);
-            const float2 a = S(pt, n1), b = S(H + pt, N1 - 1 - n1);
-            S(pt, n1) = real_merge(a, b, w);
-            S(H + pt, N1 - 1 - n1) = real_merge(b, a, make_float2(-w.x, w.y));
-        }
-    }
-    __syncthreads();
+    // Each thread merges its own elements k = N2 n1 + n2 (rows n1 = t + mT of
+    // column n2) into registers, reading the partner X[M - k] from the
+    // staged tile: row N1 - 1 - n1 of the mirror column (column 0: row
+    // N1 - n1, and X[M] at row 0).  Twiddle W_2M^k = W_2N1^n1 * W_2M^n2: a
+    // row factor from the short 2N1 level of the table, one column factor
+    // per thread.
+    const bool edge = u == 0 && (c == 0 || c == H);       // columns 0 and N2/2 mirror themselves
+    const int mc = edge ? c : (c < H ? c + H : c - H);     // slot of the mirror column
+    const float2* twr = tw + 2 * N1;                       // W_2N1^n1
+    const float2 wcol = __ldg(twn + n2);
     float2 v[P::R];
 #pragma unroll
-    for (int m = 0; m < P::R; ++m) v[m] = S(c, t + m * P::T);
+    for (int m = 0; m < P::R; ++m) {
+        const int n1 = t + m * P::T;
+        const float2 a = smem[TileView<P::C>::slot(n1, c)];
+        float2 b;
+        if (u == 0 && c == 0) b = n1 == 0 ? xm : smem[TileView<P::C>::slot(N1 - n1, 0)];
+        else b = smem[TileView<P::C>::slot(N1 - 1 - n1, mc)];
+        v[m] = real_merge(a, b, cmul(__ldg(twr + n1), wcol));
+    }
     __syncthreads();
     TileView<P::C> view{smem, c};
     stockham<LA, P::LOG2R, true, false>(v, t, tw, view);
