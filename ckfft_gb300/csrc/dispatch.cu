@@ -20,6 +20,7 @@ cudaError_t prepare_strided();
 cudaError_t prepare_fused();
 cudaError_t prepare_inter();
 cudaError_t prepare_l2pass();
+cudaError_t prepare_groups();
 
 // Opt-in (CKFFT_CUDA_CLUSTER=1): measured slower than the default paths on
 // GB300 (2^14: 2366 vs 3669 GB/s single CTA; 2^15 / 2^16: 1936 / 1516 vs about
@@ -194,6 +195,7 @@ cudaError_t prepare_device()
     if ((e = prepare_fused()) != cudaSuccess) return e;
     if ((e = prepare_inter()) != cudaSuccess) return e;
     if ((e = prepare_l2pass()) != cudaSuccess) return e;
+    if ((e = prepare_groups()) != cudaSuccess) return e;
     if (dev < 64) done |= 1ull << dev;
     return cudaSuccess;
 }

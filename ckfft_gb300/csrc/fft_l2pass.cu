@@ -19,6 +19,7 @@
 #include <cooperative_groups.h>
 
 #include "fft_passes.cuh"
+#include "jobs.h"
 #include "kernels.h"
 
 namespace cg = cooperative_groups;
@@ -85,10 +86,12 @@ __device__ __forceinline__ void merge_phase(const float2* __restrict__ x, float2
 //         bins into the intermediate first, then the complex inverse.
 // (Real forward runs as two batched passes with the split fused into the
 // row pass, which measured faster than a split phase here.)
+// fr != nullptr: transform f reads fr[f].in and writes fr[f].out (a grouped
+// launch of a job run) instead of in + f in_dist, out + f out_dist.
 template <int LA, int LB, int KIND>
 __global__ void __cluster_dims__(kL2Cluster, 1, 1) __launch_bounds__(kL2Threads, 4)
 k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __restrict__ scratch, long long in_dist,
-         long long out_dist, const float2* __restrict__ tw)
+         long long out_dist, const float2* __restrict__ tw, const FrameDesc* __restrict__ fr)
 {
     using C = L2Cfg<LA, LB>;
     constexpr bool INV = KIND == 1 || KIND == 3;
@@ -99,8 +102,8 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     const long long f = blockIdx.x / kL2Cluster;
     extern __shared__ __align__(128) float2 smem[];
     pdl_start();
-    const float2* x = in + f * in_dist;
-    float2* y = out + f * out_dist;
+    const float2* x = fr ? fr[f].in : in + f * in_dist;
+    float2* y = fr ? fr[f].out : out + f * out_dist;
     float2* s = scratch + f * n;
     const float2* twn = tw + 2 * n;                  // W_(2n): merge twiddles
 
@@ -130,11 +133,11 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
 
 template <int LA, int LB, int KIND>
 static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, long long count, long long in_dist,
-                               long long out_dist, const float2* tw, cudaStream_t s)
+                               long long out_dist, const float2* tw, cudaStream_t s, const FrameDesc* fr = nullptr)
 {
     using C = L2Cfg<LA, LB>;
     return launch_pdl(k_l2_c2c<LA, LB, KIND>, dim3((unsigned)(count * kL2Cluster)), dim3(kL2Threads), C::SMEM, s, in,
-                      out, scratch, in_dist, out_dist, tw);
+                      out, scratch, in_dist, out_dist, tw, fr);
 }
 
 bool l2pass_supported(int log2n) { return log2n >= 15 && log2n <= 16; }
@@ -162,6 +165,35 @@ cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long l
     case 0: e = launch_l2_L<LA, LB, 0>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
     case 1: e = launch_l2_L<LA, LB, 1>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
     default: e = launch_l2_L<LA, LB, 3>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;          \
+    }
+        if (log2n == 15) { CKG_L2_KIND(7, 8) }
+        else { CKG_L2_KIND(8, 8) }
+#undef CKG_L2_KIND
+        if (e != cudaSuccess) return e;
+        count_launch();
+    }
+    return cudaSuccess;
+}
+
+// The same over a table of transforms (a grouped launch of a job run).
+cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
+                                void* scratch, size_t scratch_bytes, cudaStream_t s)
+{
+    if (!l2pass_supported(log2n) || (kind != 0 && kind != 1 && kind != 3)) return cudaErrorInvalidValue;
+    if (count <= 0) return cudaSuccess;
+    const long long n = 1ll << log2n;
+    const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
+    if (group < 1 || ((uintptr_t)scratch & 127)) return cudaErrorInvalidValue;
+    float2* tmp = (float2*)scratch;
+    for (long long off = 0; off < count; off += group) {
+        const long long cnt = count - off < group ? count - off : group;
+        const FrameDesc* g = fr + off;
+        cudaError_t e;
+#define CKG_L2_KIND(LA, LB)                                                                              \
+    switch (kind) {                                                                                      \
+    case 0: e = launch_l2_L<LA, LB, 0>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;               \
+    case 1: e = launch_l2_L<LA, LB, 1>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;               \
+    default: e = launch_l2_L<LA, LB, 3>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;              \
     }
         if (log2n == 15) { CKG_L2_KIND(7, 8) }
         else { CKG_L2_KIND(8, 8) }

@@ -53,6 +53,20 @@ struct FrameDesc {
     float2* out;
 };
 
+// Grouped launches (fft_groups.cu): the transforms of one (op, log2a) of a
+// job run in one launch over a FrameDesc table.  op is a single-CTA op
+// (U_C2C_FWD .. U_C2R); log2a as for units.
+bool group_supported(int op, int log2a);
+// Scratch of a group of `count` transforms (cluster two-pass groups: at
+// most kGroupMaxL2Transforms transforms per launch).
+constexpr long long kGroupMaxL2Transforms = 1024;
+size_t group_scratch_bytes(int op, int log2a, long long count);
+cudaError_t launch_group(int op, int log2a, const FrameDesc* fr, long long count, const float2* tw,
+                         void* scratch, size_t scratch_bytes, cudaStream_t s);
+cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
+                                void* scratch, size_t scratch_bytes, cudaStream_t s);
+cudaError_t prepare_groups();
+
 struct LargeDesc {
     const float2* in;
     float2* out;

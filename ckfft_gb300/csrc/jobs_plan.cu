@@ -62,14 +62,28 @@ static int single_threads(int l)
 }
 
 
+// A grouped launch: `count` transforms of one (op, log2a), their pointers at
+// gframes[first ..], scratch at scratch_off (float2 elements) when needed.
+struct GroupSpec {
+    int op;
+    int log2a;
+    int first;
+    int count;
+    long long scratch_off;
+    size_t scratch_bytes;
+};
+
 struct Built {
     std::vector<Unit> units;
     std::vector<FrameDesc> frames;
     std::vector<LargeDesc> large;   // scratch pointers relative (offset in float2) until placed
     std::vector<long long> scratch_off;
+    std::vector<GroupSpec> groups;
+    std::vector<FrameDesc> gframes;
     long long scratch_elems = 0;
     long long algo_bytes = 0;
     long long transforms = 0;
+    bool empty() const { return units.empty() && groups.empty(); }
 };
 
 static int ilog2ll(long long n)
@@ -150,6 +164,7 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
         return false;
     }
     std::map<std::pair<int, int>, std::vector<FrameDesc>> buckets;   // (op, log2a) -> frames
+    std::map<std::pair<int, int>, std::vector<FrameDesc>> gbuckets;  // grouped launches
     std::vector<std::array<std::vector<Unit>, 2>> phases;           // per multi-pass transform
     for (int j = 0; j < njobs; ++j) {
         const CkFftCudaJob& J = jobs[j];
@@ -168,8 +183,11 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
         for (int f = 0; f < J.count; ++f) {
             const float2* in = (const float2*)((const char*)J.input + (size_t)f * in_stride_bytes);
             float2* out = (float2*)((char*)J.output + (size_t)f * out_stride_bytes);
+            const int sop = real ? (inverse ? U_C2R : U_R2C) : (inverse ? U_C2C_INV : U_C2C_FWD);
             if (real && J.n <= 4) {
                 buckets[{inverse ? U_RTINY_INV : U_RTINY_FWD, L}].push_back({in, out});
+            } else if (group_supported(sop, lc)) {
+                gbuckets[{sop, lc}].push_back({in, out});
             } else if (lc <= kJobMaxSingleLog2) {
                 const int op = real ? (inverse ? U_C2R : U_R2C) : (inverse ? U_C2C_INV : U_C2C_FWD);
                 buckets[{op, lc}].push_back({in, out});
@@ -204,6 +222,18 @@ static bool build_units(const ContextView& cv, const CkFftCudaJob* jobs, int njo
                          B_SCRATCH, B_OUT);
             }
         }
+    }
+    // Grouped launches: one per (op, log2a), largest first.
+    for (auto it = gbuckets.rbegin(); it != gbuckets.rend(); ++it) {
+        const std::vector<FrameDesc>& fr = it->second;
+        GroupSpec g{it->first.first, it->first.second, (int)b->gframes.size(), (int)fr.size(), 0, 0};
+        g.scratch_bytes = group_scratch_bytes(g.op, g.log2a, g.count);
+        if (g.scratch_bytes) {
+            g.scratch_off = b->scratch_elems;
+            b->scratch_elems += (long long)((g.scratch_bytes / sizeof(float2) + 15) / 16 * 16);
+        }
+        b->groups.push_back(g);
+        b->gframes.insert(b->gframes.end(), fr.begin(), fr.end());
     }
     // Single-CTA units, largest frames first.
     std::vector<Unit> singles;
@@ -324,6 +354,37 @@ static void make_records(const Built& b, float2* scratch, std::vector<UnitRec>* 
     }
 }
 
+// Device layout of a run: unit records | counters + queue head | the grouped
+// launches' frame tables.
+struct RunLayout {
+    size_t recs, done, gframes, total;
+};
+
+static RunLayout run_layout(const Built& b)
+{
+    RunLayout l{};
+    size_t off = 0;
+    l.recs = off; off += sizeof(UnitRec) * b.units.size();
+    off = (off + 15) / 16 * 16;
+    l.done = off; off += sizeof(int) * (b.large.size() + 1);
+    off = (off + 15) / 16 * 16;
+    l.gframes = off; off += sizeof(FrameDesc) * b.gframes.size();
+    l.total = off + 16;
+    return l;
+}
+
+// The run's grouped launches, in order, on `s` (frame tables on the device).
+static cudaError_t launch_groups(const Built& b, const FrameDesc* dframes, float2* scratch, const float2* tw,
+                                 cudaStream_t s)
+{
+    for (const GroupSpec& g : b.groups) {
+        cudaError_t e = launch_group(g.op, g.log2a, dframes + g.first, g.count, tw, scratch + g.scratch_off,
+                                     g.scratch_bytes, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 void free_run_slot(RunSlot* r)
 {
     cudaFree(r->dev);
@@ -349,12 +410,9 @@ int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunS
 {
     Built b;
     if (!build_units(cv, jobs, njobs, &b)) return 0;
-    if (b.units.empty()) return 1;
-    size_t off = 0;
-    const size_t o_recs = off; off += sizeof(UnitRec) * b.units.size();
-    off = (off + 15) / 16 * 16;
-    const size_t o_done = off; off += sizeof(int) * (b.large.size() + 1);
-    const size_t total = off + 16;
+    if (b.empty()) return 1;
+    const RunLayout lay = run_layout(b);
+    const size_t o_recs = lay.recs, o_done = lay.done, total = lay.total;
     cudaError_t e = cudaSuccess;
     if (r->host_cap < total) {
         cudaFreeHost(r->host);
@@ -375,6 +433,7 @@ int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunS
     make_records(b, scratch, &recs);
     memcpy(r->host + o_recs, recs.data(), sizeof(UnitRec) * recs.size());
     memset(r->host + o_done, 0, sizeof(int) * (b.large.size() + 1));
+    if (!b.gframes.empty()) memcpy(r->host + lay.gframes, b.gframes.data(), sizeof(FrameDesc) * b.gframes.size());
     char* base = (char*)r->dev;
     JobsArgs a{};
     a.recs = (const UnitRec*)(base + o_recs);
@@ -384,12 +443,15 @@ int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunS
     a.tw = cv.tw;
     a.err = device_error_word();
     e = cudaMemcpyAsync(r->dev, r->host, total, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = launch_jobs(a, s);
+    if (e == cudaSuccess) e = launch_groups(b, (const FrameDesc*)(base + lay.gframes), scratch, cv.tw, s);
+    if (e == cudaSuccess && !b.units.empty()) {
+        e = launch_jobs(a, s);
+        if (e == cudaSuccess) count_launch();
+    }
     if (e != cudaSuccess) {
         set_last_error(cudaGetErrorString(e));
         return -1;
     }
-    count_launch();
     return 1;
 }
 
@@ -408,6 +470,14 @@ struct _CkFftCudaPlan {
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    bool work = false;           // units or grouped launches to run
+    int kernels = 0;             // kernel nodes of the graph (launches per replay)
+    // graph branches: grouped launches on side streams, concurrent with the
+    // persistent kernel and with each other (no launch waits for another's tail)
+    static constexpr int kBranches = 4;
+    cudaStream_t side[kBranches] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kBranches] = {};
     long long algo_bytes = 0;
     long long transforms = 0;
 };
@@ -420,13 +490,10 @@ size_t align_up(size_t x) { return (x + alignof(T) - 1) / alignof(T) * alignof(T
 // Lays out the built queue in one device allocation.  `dmem` receives the
 // allocation, `scratch` the multi-pass intermediates.
 cudaError_t upload(const Built& b, ContextView cv, void** dmem, float2** scratch, JobsArgs* a, size_t* counters_bytes,
-                   cudaStream_t s, bool async_alloc)
+                   const FrameDesc** dframes, cudaStream_t s, bool async_alloc)
 {
-    size_t off = 0;
-    const size_t o_recs = off; off += sizeof(UnitRec) * b.units.size();
-    off = (off + 15) / 16 * 16;
-    const size_t o_done = off; off += sizeof(int) * (b.large.size() + 1);   // + queue head
-    const size_t total = off + 16;
+    const RunLayout lay = run_layout(b);
+    const size_t o_recs = lay.recs, o_done = lay.done, total = lay.total;
     cudaError_t e = async_alloc ? pool_alloc_async(dmem, total, s) : dev_malloc(dmem, total);
     if (e != cudaSuccess) return e;
     *scratch = nullptr;
@@ -439,6 +506,7 @@ cudaError_t upload(const Built& b, ContextView cv, void** dmem, float2** scratch
     std::vector<UnitRec> recs;
     make_records(b, *scratch, &recs);
     memcpy(host.data() + o_recs, recs.data(), sizeof(UnitRec) * recs.size());
+    if (!b.gframes.empty()) memcpy(host.data() + lay.gframes, b.gframes.data(), sizeof(FrameDesc) * b.gframes.size());
     // pageable source: the call returns once the data is staged, so `host` may go
     e = cudaMemcpyAsync(*dmem, host.data(), total, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return e;
@@ -450,6 +518,7 @@ cudaError_t upload(const Built& b, ContextView cv, void** dmem, float2** scratch
     a->tw = cv.tw;
     a->err = device_error_word();
     *counters_bytes = sizeof(int) * (b.large.size() + 1);
+    *dframes = (const FrameDesc*)(base + lay.gframes);
     return cudaSuccess;
 }
 
@@ -490,18 +559,52 @@ CkFftCudaPlan* CkFftCudaPlanJobs(CkFftContext* context, const CkFftCudaJob* jobs
     p->nlarge = (int)b.large.size();
     p->algo_bytes = b.algo_bytes;
     p->transforms = b.transforms;
+    p->work = !b.empty();
+    const FrameDesc* dframes = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = upload(b, cv, &p->dmem, &p->scratch, &p->args, &p->counters_bytes, p->stream, false);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+    for (int i = 0; i < _CkFftCudaPlan::kBranches && e == cudaSuccess; ++i) {
+        e = cudaStreamCreateWithFlags(&p->side[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->join[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess)
+        e = upload(b, cv, &p->dmem, &p->scratch, &p->args, &p->counters_bytes, &dframes, p->stream, false);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
-    if (e == cudaSuccess && p->nunits > 0) {
+    const long long counted = launch_count();       // launches counted while capturing are not run
+    if (e == cudaSuccess && p->work) {
         e = cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t e1 = cudaMemsetAsync(p->args.done, 0, p->counters_bytes, p->stream);
-            cudaError_t e2 = e1 == cudaSuccess ? launch_jobs(p->args, p->stream) : e1;
+            // grouped launches round-robin on the side branches, the
+            // persistent kernel over the units on the main one
+            cudaError_t e1 = cudaEventRecord(p->fork, p->stream);
+            const int nb = (int)std::min<size_t>(b.groups.size(), _CkFftCudaPlan::kBranches);
+            for (int i = 0; i < nb && e1 == cudaSuccess; ++i) e1 = cudaStreamWaitEvent(p->side[i], p->fork, 0);
+            for (size_t g = 0; g < b.groups.size() && e1 == cudaSuccess; ++g) {
+                const GroupSpec& G = b.groups[g];
+                e1 = launch_group(G.op, G.log2a, dframes + G.first, G.count, cv.tw, p->scratch + G.scratch_off,
+                                  G.scratch_bytes, p->side[g % _CkFftCudaPlan::kBranches]);
+            }
+            if (e1 == cudaSuccess) e1 = cudaMemsetAsync(p->args.done, 0, p->counters_bytes, p->stream);
+            if (e1 == cudaSuccess && p->nunits > 0) e1 = launch_jobs(p->args, p->stream);
+            for (int i = 0; i < nb && e1 == cudaSuccess; ++i) {
+                e1 = cudaEventRecord(p->join[i], p->side[i]);
+                if (e1 == cudaSuccess) e1 = cudaStreamWaitEvent(p->stream, p->join[i], 0);
+            }
+            cudaError_t e2 = e1;
             e = cudaStreamEndCapture(p->stream, &p->graph);
             if (e == cudaSuccess) e = e2;
         }
         if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+        count_launch((int)(counted - launch_count()));
+        size_t nn = 0;
+        if (e == cudaSuccess) e = cudaGraphGetNodes(p->graph, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (e == cudaSuccess && nn) e = cudaGraphGetNodes(p->graph, nodes.data(), &nn);
+        for (size_t i = 0; i < nn && e == cudaSuccess; ++i) {
+            cudaGraphNodeType t;
+            e = cudaGraphNodeGetType(nodes[i], &t);
+            if (e == cudaSuccess && t == cudaGraphNodeTypeKernel) ++p->kernels;
+        }
     }
     if (e != cudaSuccess) {
         fail_cuda("planning the job run", e);
@@ -514,13 +617,13 @@ CkFftCudaPlan* CkFftCudaPlanJobs(CkFftContext* context, const CkFftCudaJob* jobs
 int CkFftCudaExecPlan(CkFftCudaPlan* p, void* stream)
 {
     if (!p) { set_last_error("NULL plan"); return 0; }
-    if (p->nunits == 0) return 1;
+    if (!p->work) return 1;
     DevScope scope(p->cv.device);
     if (!scope.ok) { set_last_error("cannot select the plan's device"); return 0; }
     cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
     cudaError_t e = cudaGraphLaunch(p->exec, s);
     if (e != cudaSuccess) return fail_cuda("cudaGraphLaunch", e);
-    count_launch();
+    count_launch(p->kernels);
     if (!stream) {
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return fail_cuda("cudaStreamSynchronize", e);
@@ -538,6 +641,11 @@ void CkFftCudaDestroyPlan(CkFftCudaPlan* p)
     if (p->graph) cudaGraphDestroy(p->graph);
     cudaFree(p->dmem);
     cudaFree(p->scratch);
+    for (int i = 0; i < _CkFftCudaPlan::kBranches; ++i) {
+        if (p->side[i]) cudaStreamDestroy(p->side[i]);
+        if (p->join[i]) cudaEventDestroy(p->join[i]);
+    }
+    if (p->fork) cudaEventDestroy(p->fork);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -552,15 +660,17 @@ int CkFftCudaRunJobs(CkFftContext* context, const CkFftCudaJob* jobs, int njobs,
     if (!scope.ok) { set_last_error("cannot select the context's device"); return 0; }
     Built b;
     if (!build_units(cv, jobs, njobs, &b)) return 0;
-    if (b.units.empty()) return 1;
+    if (b.empty()) return 1;
     cudaStream_t s = (cudaStream_t)stream;
     void* dmem = nullptr;
     float2* scratch = nullptr;
     JobsArgs a{};
     size_t cb = 0;
-    cudaError_t e = upload(b, cv, &dmem, &scratch, &a, &cb, s, true);
+    const FrameDesc* dframes = nullptr;
+    cudaError_t e = upload(b, cv, &dmem, &scratch, &a, &cb, &dframes, s, true);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.done, 0, cb, s);
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess) e = launch_groups(b, dframes, scratch, cv.tw, s);
+    if (e == cudaSuccess && !b.units.empty()) {
         e = launch_jobs(a, s);
         if (e == cudaSuccess) count_launch();
     }
