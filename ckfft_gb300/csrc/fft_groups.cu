@@ -79,14 +79,15 @@ static cudaError_t launch_table(int l, const FrameDesc* fr, long long count, con
 
 // Sizes the job kernel runs as two phases of pass units (log2a above
 // kJobMaxSingleLog2) and a batched kernel runs in one launch: single-CTA up
-// to 2^14, the cluster two-pass kernel at 2^15 / 2^16 (real: inverse only).
+// to 2^14, the cluster two-pass kernel at 2^15 / 2^16 (complex, real
+// inverse), two passes with the split fused at 2^15 / 2^16 (real forward).
 bool group_supported(int op, int log2a)
 {
     if (log2a <= kJobMaxSingleLog2) return false;
     switch (op) {
     case U_C2C_FWD:
     case U_C2C_INV: return log2a <= 14 || l2pass_supported(log2a);
-    case U_R2C: return log2a <= 14;
+    case U_R2C: return log2a <= 16;
     case U_C2R: return log2a <= 14 || l2pass_supported(log2a);
     default: return false;
     }
@@ -94,7 +95,7 @@ bool group_supported(int op, int log2a)
 
 size_t group_scratch_bytes(int op, int log2a, long long count)
 {
-    if (log2a <= 14 || !(op == U_C2C_FWD || op == U_C2C_INV || op == U_C2R)) return 0;
+    if (log2a <= 14 || !(op == U_C2C_FWD || op == U_C2C_INV || op == U_R2C || op == U_C2R)) return 0;
     const long long per_launch = count < kGroupMaxL2Transforms ? count : kGroupMaxL2Transforms;
     return sizeof(float2) * ((size_t)per_launch << log2a);
 }
@@ -103,6 +104,7 @@ cudaError_t launch_group(int op, int log2a, const FrameDesc* fr, long long count
                          void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
     if (count <= 0) return cudaSuccess;
+    if (log2a > 14 && op == U_R2C) return launch_r2c_table(log2a, fr, count, tw, scratch, scratch_bytes, s);
     if (log2a > 14) {
         const int kind = op == U_C2C_FWD ? 0 : op == U_C2C_INV ? 1 : op == U_C2R ? 3 : -1;
         if (kind < 0) return cudaErrorInvalidValue;
