@@ -139,6 +139,32 @@ def test_plan_replays_and_reads_current_inputs(torch_cuda, ctx_cache, oracle_mod
     plan.close()
 
 
+def test_plan_groups_multi_pass_sizes(torch_cuda, ctx_cache, oracle_mod):
+    """Transforms the job kernel would split into pass units run as grouped
+    launches over pointer tables (single-CTA tables at complex 2^13 / real
+    2^15, the cluster kernel at complex 2^15 and real inverse 2^16, the fused
+    two-pass real forward at 2^16), beside the persistent kernel that takes
+    the small ones: one replay launches exactly those kernels."""
+    from ckfft_gb300 import binding
+    torch = torch_cuda
+    rng = np.random.default_rng(5)
+    spec = [("cfwd", 1 << 13, 3), ("rfwd", 1 << 15, 2), ("cinv", 1 << 15, 3), ("rinv", 1 << 16, 2),
+            ("rfwd", 1 << 16, 3), ("cfwd", 256, 7), ("rinv", 64, 5)]
+    jobs = [make_job(torch, rng, k, n, c) for k, n, c in spec]
+    ctx = ctx_cache(1 << 16)
+    plan = ctx.plan([as_tuple(j) for j in jobs])
+    before = binding.launch_count()
+    ctx.check(plan.exec(), "exec")
+    # 2 single-CTA tables + 2 cluster launches + 2 passes (real forward 2^16) + the job kernel
+    assert binding.launch_count() - before == 7
+    o = oracle_mod.Oracle(1 << 16)
+    for j in jobs:
+        got = j["out"].cpu().numpy()
+        for f in range(j["count"]):
+            assert_close(got[f], oracle_out(o, j, f), j["n"], f"grouped {j['kind']} {j['n']}")
+    plan.close()
+
+
 def test_workload4_sample(torch_cuda, ctx_cache, oracle_mod):
     """The uneven batch: 10000 transforms, log2 n in 6..16, 70% complex, 50% inverse."""
     from ckfft_gb300 import workloads as wl
