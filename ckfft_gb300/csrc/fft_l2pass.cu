@@ -1,5 +1,6 @@
-// fft_l2pass.cu -- complex 2^15 and 2^16 (and real inverse 2^16, 2^17) in
-// two passes whose intermediate never reaches HBM.
+// fft_l2pass.cu -- complex 2^15 and 2^16 (and, for grouped launches of job
+// runs, real inverse 2^16, 2^17) in two passes whose intermediate never
+// reaches HBM.
 //
 // The multi-pass transform of fft_large.cu (columns, then rows, see
 // fft_passes.cuh) runs here inside one thread-block cluster of K CTAs per
@@ -13,9 +14,11 @@
 // on GB300 (batches of 1 GiB): 2^15 3328 vs 3145 GB/s, 2^16 3439 vs 3105;
 // the kernel is then bound by the two passes' instructions, not by HBM (40 %
 // DRAM throughput, no intermediate bytes in DRAM).  At 2^17 it was slower
-// (2779 vs 2857) and is not used there.  Real inverse 2^16 / 2^17 runs the
-// merge as a first phase of the same cluster: 2381 / 2456 GB/s, against
-// 2206 / 2089 with the merge fused into the batched column pass.
+// (2779 vs 2857) and is not used there.  The real inverse (KIND 3) runs the
+// merge as a first phase of the same cluster; batched real inverses use the
+// merge fused into the two-pass column pass instead (2607 / 2454 GB/s at
+// 2^16 / 2^17 against 2262 / 2439 here), grouped launches of job runs this
+// kernel with its pointer table.
 #include <cooperative_groups.h>
 
 #include "fft_passes.cuh"
