@@ -630,8 +630,9 @@ def run_sizes(args):
 
 
 def run_w4(args):
-    """Workload 4: 10000 transforms of uneven sizes in one graph-captured persistent launch,
-    against the plain path of one CkFft* call per transform."""
+    """Workload 4: 10000 transforms of uneven sizes in one graph replay (the persistent job
+    kernel plus grouped launches over pointer tables), against the plain path of one CkFft*
+    call per transform."""
     import numpy as np
     import torch
     from ckfft_gb300 import binding
@@ -692,12 +693,15 @@ def run_w4(args):
     peak, src = measured_peaks()
     line = base_line(args, "uneven batch FFT GB/s (10000 transforms, log2 n 6..16, mixed kinds)", value, "GB/s", secs,
                      {"workload": "10000 transforms, log2 n uniform 6..16, 70% complex / 30% real, 50% inverse, "
-                                  "U[-1,1) inputs, one CUDA-graph replay of the persistent job kernel per step",
+                                  "U[-1,1) inputs, one CUDA-graph replay per step (the persistent job kernel for "
+                                  "complex <= 2^12 / real <= 2^13, grouped launches over pointer tables above)",
                       "jobs": len(jobs), "l2": f"{plan.bytes / 1e9:.2f} GB of algorithmic traffic per step (larger than L2)"})
     line["transforms_per_s"] = round(tps, 1)
-    line["roofline"] = {"bound": "hbm", "kernel": "k_jobs (persistent job kernel)", "achieved": round(value, 1),
-                        "peak": peak, "unit": "GB/s", "frac": round(value / peak, 4), "peak_source": src,
-                        "traffic": None, "note": "multi-pass jobs (2^14..2^16) move 2x their algorithmic bytes"}
+    line["roofline"] = {"bound": "hbm", "kernel": "one graph: k_jobs + grouped k_l2_c2c / k_*_table launches",
+                        "achieved": round(value, 1), "peak": peak, "unit": "GB/s", "frac": round(value / peak, 4),
+                        "peak_source": src, "traffic": None,
+                        "note": "complex 2^15 / 2^16 (60% of the bytes) run the cluster two-pass kernel: one DRAM "
+                                "pass, two passes of instructions"}
     if pc is not None:
         line["per_call"] = {"transforms_per_s": round(len(jobs) / pc, 1), "gbs": round(plan.bytes / pc / 1e9, 2),
                             "api": "one CkFftComplex*/CkFftReal* call per transform (device pointers, blocking)",

@@ -1,9 +1,11 @@
 // jobs_plan.cu -- host side of mixed runs: CkFftCudaPlanJobs / ExecPlan / RunJobs.
 //
 // Turns a list of jobs (kind, size, count, device pointers) into the unit
-// queue of the persistent job kernel (jobs.h), uploads it once, and captures
-// "reset counters + persistent launch" into a CUDA graph, so a replay costs one
-// graph launch regardless of how many transforms the run holds.
+// queue of the persistent job kernel (jobs.h) and the pointer tables of the
+// grouped launches (fft_groups.cu), uploads them once, and captures
+// "reset counters + grouped launches on side branches + persistent launch"
+// into a CUDA graph, so a replay costs one graph launch regardless of how
+// many transforms the run holds.
 #include <algorithm>
 #include <array>
 #include <cstring>

@@ -191,7 +191,11 @@ long long CkFftCudaLaunchCount(void);
 
 /* ----------------------------------------------------------------------
  * Mixed runs: many transforms of different sizes, kinds and directions in
- * one persistent kernel launch (no counterpart in the reference).
+ * one call or one graph replay (no counterpart in the reference): a
+ * persistent kernel over a device work queue takes the small transforms,
+ * and each (kind, size) that a batched kernel runs in one launch (complex
+ * 2^13..2^16, real 2^14..2^17) is one launch over a table of the jobs'
+ * pointers.
  * ---------------------------------------------------------------------- */
 
 #define CKFFT_CUDA_COMPLEX_FORWARD 0
@@ -216,8 +220,10 @@ CkFftCudaJob;
 typedef struct _CkFftCudaPlan CkFftCudaPlan;
 
 /* Validates the jobs (same rules and errors as the single calls), builds the
- * device work queue, allocates the multi-pass intermediates and captures the
- * run into a CUDA graph.  Returns NULL on error (see CkFftCudaGetLastError). */
+ * device work queue and pointer tables, allocates the multi-pass
+ * intermediates and captures the run into a CUDA graph (the table launches
+ * on parallel branches beside the persistent kernel).  Returns NULL on error
+ * (see CkFftCudaGetLastError). */
 CkFftCudaPlan* CkFftCudaPlanJobs(CkFftContext* context, const CkFftCudaJob* jobs, int njobs);
 
 /* Replays a plan: one graph launch.  stream NULL blocks until done; otherwise

@@ -1,5 +1,6 @@
 """GPU tests of mixed runs (CkFftCudaPlanJobs / ExecPlan / RunJobs): many
-transforms of different sizes, kinds and directions in one persistent launch.
+transforms of different sizes, kinds and directions in one call or graph
+replay (the persistent job kernel plus grouped launches over pointer tables).
 Each result must equal the oracle within the parity bar, and must be the same
 bits alone and in the mix."""
 import numpy as np
