@@ -3,8 +3,9 @@
 // hardware-scheduled launch that reads each transform's input and output
 // pointers from a table (FrameDesc), instead of as units of the persistent
 // kernel.  The frame bodies are the batched kernels' (fft_small.cuh); the
-// 2^15 / 2^16 complex (and 2^16 real inverse) groups use the cluster
-// two-pass kernel with its table argument (fft_l2pass.cu).
+// 2^15 / 2^16 complex groups use the cluster two-pass kernel with its table
+// argument (fft_l2pass.cu), real 2^16 / 2^17 the two-pass kernels with the
+// split / merge fused (fft_large.cu).
 #include "fft_small.cuh"
 #include "jobs.h"
 #include "kernels.h"
@@ -79,8 +80,8 @@ static cudaError_t launch_table(int l, const FrameDesc* fr, long long count, con
 
 // Sizes the job kernel runs as two phases of pass units (log2a above
 // kJobMaxSingleLog2) and a batched kernel runs in one launch: single-CTA up
-// to 2^14, the cluster two-pass kernel at 2^15 / 2^16 (complex, real
-// inverse), two passes with the split fused at 2^15 / 2^16 (real forward).
+// to 2^14, the cluster two-pass kernel at 2^15 / 2^16 (complex), two passes
+// with the split / merge fused at 2^15 / 2^16 (real).
 bool group_supported(int op, int log2a)
 {
     if (log2a <= kJobMaxSingleLog2) return false;
@@ -88,7 +89,7 @@ bool group_supported(int op, int log2a)
     case U_C2C_FWD:
     case U_C2C_INV: return log2a <= 14 || l2pass_supported(log2a);
     case U_R2C: return log2a <= 16;
-    case U_C2R: return log2a <= 14 || l2pass_supported(log2a);
+    case U_C2R: return log2a <= 16;
     default: return false;
     }
 }
@@ -105,10 +106,10 @@ cudaError_t launch_group(int op, int log2a, const FrameDesc* fr, long long count
 {
     if (count <= 0) return cudaSuccess;
     if (log2a > 14 && op == U_R2C) return launch_r2c_table(log2a, fr, count, tw, scratch, scratch_bytes, s);
+    if (log2a > 14 && op == U_C2R) return launch_c2r_table(log2a, fr, count, tw, scratch, scratch_bytes, s);
     if (log2a > 14) {
-        const int kind = op == U_C2C_FWD ? 0 : op == U_C2C_INV ? 1 : op == U_C2R ? 3 : -1;
-        if (kind < 0) return cudaErrorInvalidValue;
-        return launch_l2pass_table(kind, log2a, fr, count, tw, scratch, scratch_bytes, s);
+        if (op != U_C2C_FWD && op != U_C2C_INV) return cudaErrorInvalidValue;
+        return launch_l2pass_table(op == U_C2C_INV ? 1 : 0, log2a, fr, count, tw, scratch, scratch_bytes, s);
     }
     cudaError_t e;
     switch (op) {

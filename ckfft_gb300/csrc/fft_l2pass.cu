@@ -1,6 +1,5 @@
-// fft_l2pass.cu -- complex 2^15 and 2^16 (and, for grouped launches of job
-// runs, real inverse 2^16, 2^17) in two passes whose intermediate never
-// reaches HBM.
+// fft_l2pass.cu -- complex 2^15 and 2^16 in two passes whose intermediate
+// never reaches HBM.
 //
 // The multi-pass transform of fft_large.cu (columns, then rows, see
 // fft_passes.cuh) runs here inside one thread-block cluster of K CTAs per
@@ -14,11 +13,11 @@
 // on GB300 (batches of 1 GiB): 2^15 3328 vs 3145 GB/s, 2^16 3439 vs 3105;
 // the kernel is then bound by the two passes' instructions, not by HBM (40 %
 // DRAM throughput, no intermediate bytes in DRAM).  At 2^17 it was slower
-// (2779 vs 2857) and is not used there.  The real inverse (KIND 3) runs the
-// merge as a first phase of the same cluster; batched real inverses use the
-// merge fused into the two-pass column pass instead (2607 / 2454 GB/s at
-// 2^16 / 2^17 against 2262 / 2439 here), grouped launches of job runs this
-// kernel with its pointer table.
+// (2779 vs 2857) and is not used there.  Real transforms of these half
+// lengths run the batched two-pass kernels with the split / merge fused
+// into a pass instead: a split or merge phase inside this cluster measured
+// slower (real 2^16 forward 2109 against 2550 GB/s, inverse 2262 against
+// 2607).
 #include <cooperative_groups.h>
 
 #include "fft_passes.cuh"
@@ -58,37 +57,9 @@ __device__ __forceinline__ void cluster_barrier(cg::cluster_group& cluster)
     cluster.sync();
 }
 
-// The real inverse merge of n+1 bins x into n values s (merge_elem's algebra).
-template <long long N, int CT>
-__device__ __forceinline__ void merge_phase(const float2* __restrict__ x, float2* __restrict__ s, int idx,
-                                            const float2* __restrict__ twn)
-{
-    constexpr int PER = (int)(N / CT);
-    constexpr int B = 8;
-#pragma unroll 1
-    for (int j0 = 0; j0 < PER; j0 += B) {
-        float2 a[B], b[B];
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            const long long k = idx + (long long)(j0 + j) * CT;
-            a[j] = __ldcs(x + k);
-            b[j] = __ldg(x + (N - k));
-        }
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            const long long k = idx + (long long)(j0 + j) * CT;
-            s[k] = real_merge(a[j], b[j], __ldg(twn + k));
-        }
-    }
-}
-
 // One transform per cluster: blockIdx.x / K.  scratch holds 2^(LA+LB) values
 // per transform of the launch (128-byte aligned rows).
 // KIND 0 / 1: complex forward / inverse of n = 2^(LA+LB) points.
-// KIND 3: real inverse to 2n reals (out_dist in pairs): the merge of the n+1
-//         bins into the intermediate first, then the complex inverse.
-// (Real forward runs as two batched passes with the split fused into the
-// row pass, which measured faster than a split phase here.)
 // fr != nullptr: transform f reads fr[f].in and writes fr[f].out (a grouped
 // launch of a job run) instead of in + f in_dist, out + f out_dist.
 template <int LA, int LB, int KIND>
@@ -97,9 +68,8 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
          long long out_dist, const float2* __restrict__ tw, const FrameDesc* __restrict__ fr)
 {
     using C = L2Cfg<LA, LB>;
-    constexpr bool INV = KIND == 1 || KIND == 3;
+    constexpr bool INV = KIND == 1;
     constexpr long long n = 1ll << (LA + LB);
-    constexpr int CT = kL2Cluster * kL2Threads;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const long long f = blockIdx.x / kL2Cluster;
@@ -108,19 +78,12 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     const float2* x = fr ? fr[f].in : in + f * in_dist;
     float2* y = fr ? fr[f].out : out + f * out_dist;
     float2* s = scratch + f * n;
-    const float2* twn = tw + 2 * n;                  // W_(2n): merge twiddles
-
-    if constexpr (KIND == 3) {
-        merge_phase<n, CT>(x, s, rank * kL2Threads + threadIdx.x, twn);
-        cluster_barrier(cluster);
-    }
-    // columns: the input (or, real inverse, the merged spectrum in place) -> s
-    const float2* src = KIND == 3 ? s : x;
+    // columns: the input -> s
     const int sga = threadIdx.x / C::PA::THREADS, ta = threadIdx.x % C::PA::THREADS;
 #pragma unroll 1
     for (int i = 0; i < C::ITER_A; ++i) {
         const int tile = (i * kL2Cluster + rank) * C::SGA + sga;
-        pass_cols<LA, INV, KIND == 3, kL2Threads>(src, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
+        pass_cols<LA, INV, false, kL2Threads>(x, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
         __syncthreads();                             // the tile's shared memory is reused
     }
     // every column tile of the transform is in L2 before any row tile reads it
@@ -145,12 +108,11 @@ static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, l
 
 bool l2pass_supported(int log2n) { return log2n >= 15 && log2n <= 16; }
 
-// kind: 0 / 1 complex forward / inverse, 3 real inverse whose half length is
-// 2^log2n (dists in complex units / packed pairs).
+// kind: 0 / 1 complex forward / inverse (dists in complex units).
 cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,
                           long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
-    if (!l2pass_supported(log2n) || (kind != 0 && kind != 1 && kind != 3)) return cudaErrorInvalidValue;
+    if (!l2pass_supported(log2n) || (kind != 0 && kind != 1)) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;
     const long long n = 1ll << log2n;
     const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
@@ -166,8 +128,7 @@ cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long l
 #define CKG_L2_KIND(LA, LB)                                                                        \
     switch (kind) {                                                                                \
     case 0: e = launch_l2_L<LA, LB, 0>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
-    case 1: e = launch_l2_L<LA, LB, 1>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
-    default: e = launch_l2_L<LA, LB, 3>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;          \
+    default: e = launch_l2_L<LA, LB, 1>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;          \
     }
         if (log2n == 15) { CKG_L2_KIND(7, 8) }
         else { CKG_L2_KIND(8, 8) }
@@ -182,7 +143,7 @@ cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long l
 cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
                                 void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
-    if (!l2pass_supported(log2n) || (kind != 0 && kind != 1 && kind != 3)) return cudaErrorInvalidValue;
+    if (!l2pass_supported(log2n) || (kind != 0 && kind != 1)) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;
     const long long n = 1ll << log2n;
     const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
@@ -195,8 +156,7 @@ cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long l
 #define CKG_L2_KIND(LA, LB)                                                                              \
     switch (kind) {                                                                                      \
     case 0: e = launch_l2_L<LA, LB, 0>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;               \
-    case 1: e = launch_l2_L<LA, LB, 1>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;               \
-    default: e = launch_l2_L<LA, LB, 3>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;              \
+    default: e = launch_l2_L<LA, LB, 1>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;              \
     }
         if (log2n == 15) { CKG_L2_KIND(7, 8) }
         else { CKG_L2_KIND(8, 8) }
@@ -214,7 +174,6 @@ static cudaError_t attr_l2()
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 0>, a, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 1>, a, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 3>, a, smem);
     return e;
 }
 
