@@ -11,8 +11,10 @@
 //
 // Both passes read and write HBM once, with C adjacent columns (pass 1) or
 // rows (pass 2) per CTA so every warp access covers C*8 contiguous bytes.
-// Real sizes run the half-length complex transform plus a split (forward) or
-// merge (inverse) pass, the algebra of src/ckfft/fft_real_default.cpp.
+// Real sizes run the half-length complex transform with the split (forward)
+// fused into its last pass and the merge (inverse) into its first, the
+// algebra of src/ckfft/fft_real_default.cpp; a separate split / merge kernel
+// remains for scratch arrays that are not 128-byte aligned.
 #include <cstdint>
 
 #include "fft_passes.cuh"
@@ -187,7 +189,8 @@ k_rows_inv_table(const float2* __restrict__ tmp, const FrameDesc* __restrict__ f
         tmp + (f << (log2n1 + LB)), fr[f].out, log2n1, blockIdx.x % tiles, threadIdx.x, smem, tw);
 }
 
-// ------------------------------------------------- real split / merge passes
+// --------------------------- real split / merge as passes of their own
+// (used only when the scratch array is not 128-byte aligned)
 
 // In-place split of a natural-order half-length spectrum Z (M = 2^lm values,
 // with room for M+1) into the real forward output X[0..M].

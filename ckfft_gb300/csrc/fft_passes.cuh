@@ -244,8 +244,8 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
 // pair (k, M - k) -- k = k1 + N1 k2, M - k = (N1 - k1) + N1 (N2 - 1 - k2) --
 // are in one CTA.  After the row DFTs the tile's half-length spectrum stays
 // in shared memory and the CTA writes the bins X[k], X[M-k] (M+1 bins per
-// transform) directly: no split pass over HBM.  Same algebra and rounding as
-// split_pair_inplace.
+// transform) directly: no split pass over HBM.  Same algebra as
+// split_pair_inplace, with the twiddles factored (see below).
 // The third pass of the three-pass transform is the same pass over
 // N1 = N1' N2' rows: row k1' + N1' k2' sits at in[k1' N2' N3 + k2' N3] (the
 // intermediate of the second pass); log2k1 = log2 N1' selects that address

@@ -89,7 +89,8 @@ cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out,
                              void* scratch, size_t scratch_bytes, cudaStream_t stream);
 
 // Real transforms above the single-CTA limit: half-size multi-pass complex
-// transform plus a split (forward) or merge (inverse) pass.
+// transform with the split (forward) fused into its last pass, the merge
+// (inverse) into its first.
 cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long count,
                              long long in_dist, long long out_dist, const float2* tw,
                              void* scratch, size_t scratch_bytes, cudaStream_t stream);
