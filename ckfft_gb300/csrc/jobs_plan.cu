@@ -475,8 +475,10 @@ struct _CkFftCudaPlan {
     bool work = false;           // units or grouped launches to run
     int kernels = 0;             // kernel nodes of the graph (launches per replay)
     // graph branches: grouped launches on side streams, concurrent with the
-    // persistent kernel and with each other (no launch waits for another's tail)
-    static constexpr int kBranches = 4;
+    // persistent kernel and with each other (no launch waits for another's
+    // tail); 2 / 4 / 8 branches measured 3112 / 3247 / 3282 GB/s on the
+    // 10000-job run
+    static constexpr int kBranches = 8;
     cudaStream_t side[kBranches] = {};
     cudaEvent_t fork = nullptr;
     cudaEvent_t join[kBranches] = {};
