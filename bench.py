@@ -15,6 +15,16 @@ pair), inputs resident in HBM.  Prints one JSON line on rank 0.
   cpu_baseline  the reference's scalar path (the oracle port, or the reference
              build where it exists) on every host core, on a sample of frames
   per_call   the plain drop-in: one CkFftRealForward call (one launch) per frame
+  w4         the uneven batch (10000 transforms, log2 n 6..16, mixed kinds) in
+             one graph replay: GB/s, fraction of HBM, transforms/s against one
+             drop-in call per transform, and its CPU baseline
+  w5         serving: Poisson request streams at 10-90% of the batched peak of
+             the same request mix, p50 / p99 / p99.9 through the server and
+             through one call per request, device- and host-resident requests
+
+--gpus N must equal the launcher's WORLD_SIZE (torchrun --nproc-per-node N):
+one rank per GPU, each transforming its own shard of frames (replicas, no
+collective besides the barrier and the max of the timing).
 
 --impl reference times the reference's CPU implementation on the host cores
 for the same workload and metric (rank 0 only).
@@ -55,6 +65,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-percall", action="store_true")
+    ap.add_argument("--no-w4", action="store_true", help="default line: leave out the uneven-batch sub-object")
+    ap.add_argument("--no-w5", action="store_true", help="default line: leave out the serving sub-object")
+    ap.add_argument("--requests", type=int, default=10000, help="w5: requests per offered load")
     ap.add_argument("--direct-mb", type=int, default=8, help="w5: requests this large skip batching")
     ap.add_argument("--workload", choices=["w1", "w2", "w3", "w4", "w5", "sizes"], default="w2",
                     help="w2 (default): real n=4096 x 65536 frames; w1: complex n=1024 x 4096 round trip; "
@@ -253,8 +266,9 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     n, frames = args.n, args.frames
+    shard = frame_shard(rank, world, frames)
     ctx = binding.Context(n)
-    x = wl.sine_frames_torch(frames, n, wl.W2_SEED + rank, device=dev)
+    x = wl.sine_frames_torch(frames, n, shard["seed"], device=dev)
     X = torch.empty((frames, n // 2 + 1), dtype=torch.complex64, device=dev)
     y = torch.empty((frames, n), dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
@@ -270,10 +284,12 @@ def run_ours(args, rank, world, local_rank):
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
-    # correctness gate on the benchmarked data: round trip and one oracle frame
+    # correctness gate on the benchmarked data: the round trip, and one frame
+    # of each direction against the oracle (the inverse on the GPU's spectrum)
     err = (torch.linalg.vector_norm((y / (2 * n) - x).double()) / torch.linalg.vector_norm(x.double())).item()
     if not err < 1e-5:
         raise SystemExit(f"round-trip error {err:.3e}: refusing to report a number")
+    gate = oracle_gate(n, x[frames // 2].cpu().numpy(), X[frames // 2].cpu().numpy(), y[frames // 2].cpu().numpy())
 
     def barrier():
         if world > 1:
@@ -311,7 +327,7 @@ def run_ours(args, rank, world, local_rank):
 
     e2e = None
     if not args.no_e2e:
-        e2e = measure_e2e(torch, ctx, x, n, frames, bytes_step, world)
+        e2e = measure_e2e(torch, ctx, x, n, frames, bytes_step, world, steps=args.steps)
 
     per_call = None if args.no_percall else measure_per_call(torch, ctx, x, n)
     cpu = None
@@ -343,15 +359,35 @@ def run_ours(args, rank, world, local_rank):
         "transforms_per_s": round(world * 2 * frames * args.steps / secs, 1),
         "gflops_2.5nlog2n": round(world * 2 * frames * 2.5 * n * math.log2(n) * args.steps / secs / 1e9, 1),
         "round_trip_rel_err": err,
+        "oracle_gate": gate,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
-    print(json.dumps(line), flush=True)
     ctx.close()
+    if world == 1 and not args.no_w4:
+        line["w4"] = measure_w4(args)
+    if world == 1 and not args.no_w5:
+        line["w5"] = measure_w5(args)
+    print(json.dumps(line), flush=True)
 
 
-def measure_e2e(torch, ctx, x, n, frames, bytes_step, world, steps=3):
-    """The same step through the C ABI with pinned host buffers (copies timed)."""
+def oracle_gate(n, x, X, y):
+    """One frame of the benchmarked data against the oracle: the forward
+    spectrum of x, and the inverse of the GPU's own spectrum X."""
+    from oracle import oracle as orc
+
+    orc.build(with_reference=False)
+    o = orc.Oracle(n)
+    ef = orc.rel_l2(X, o.real_forward(n, x))
+    ei = orc.rel_l2(y, o.real_inverse(n, X))
+    if not (ef <= 1e-5 and ei <= 1e-5):
+        raise SystemExit(f"oracle gate failed: forward {ef:.3e}, inverse {ei:.3e}: refusing to report a number")
+    return {"forward_rel_l2": ef, "inverse_rel_l2": ei}
+
+
+def measure_e2e(torch, ctx, x, n, frames, bytes_step, world, steps=20):
+    """The same step through the C ABI with pinned host buffers (copies timed),
+    over as many steps as the device-timed value."""
     xh = x.cpu().pin_memory()
     Xh = torch.empty((frames, n // 2 + 1), dtype=torch.complex64).pin_memory()
     yh = torch.empty((frames, n), dtype=torch.float32).pin_memory()
@@ -383,6 +419,17 @@ def measure_per_call(torch, ctx, x, n, calls=512):
     dt = time.perf_counter() - t0
     return {"transforms_per_s": round(calls / dt, 1), "gbs": round(calls * frame_bytes(n) / dt / 1e9, 3),
             "calls": calls, "api": "CkFftRealForward per frame (device pointers, blocking)"}
+
+
+def frame_shard(rank, world, frames_per_rank, seed=None):
+    """Rank `rank`'s share of a weak-scaling run: frames [start, start + count)
+    of the job's world * frames_per_rank frames, generated from its own seed."""
+    if not (0 <= rank < world) or frames_per_rank < 0:
+        raise ValueError(f"bad shard: rank {rank} of {world}, {frames_per_rank} frames")
+    from ckfft_gb300 import workloads as wl
+
+    base = wl.W2_SEED if seed is None else seed
+    return {"start": rank * frames_per_rank, "count": frames_per_rank, "seed": base + rank}
 
 
 def combine_ranks(secs, bytes_local, world):
@@ -629,21 +676,12 @@ def run_sizes(args):
     ctx.close()
 
 
-def run_w4(args):
-    """Workload 4: 10000 transforms of uneven sizes in one graph replay (the persistent job
-    kernel plus grouped launches over pointer tables), against the plain path of one CkFft*
-    call per transform."""
-    import numpy as np
-    import torch
-    from ckfft_gb300 import binding
+def w4_jobs(torch, g):
+    """The uneven batch's 10000 jobs with U[-1,1) inputs generated on the device."""
     from ckfft_gb300 import workloads as wl
 
-    spec = wl.uneven_jobs()
-    ctx = binding.Context(1 << 16)
-    g = torch.Generator(device="cuda")
-    g.manual_seed(wl.W4_SEED)
     jobs = []
-    for real, inv, l2 in spec:
+    for real, inv, l2 in wl.uneven_jobs():
         n = 1 << l2
         if real and not inv:
             x = torch.rand(n, generator=g, device="cuda") * 2 - 1
@@ -660,18 +698,72 @@ def run_w4(args):
             y = torch.empty_like(x)
             kind = "cinv" if inv else "cfwd"
         jobs.append((kind, n, 1, x, y))
+    return jobs
+
+
+ORACLE_KIND = {"cfwd": 0, "cinv": 1, "rfwd": 2, "rinv": 3}
+
+
+def time_cpu_jobs(groups, min_seconds=2.0):
+    """The reference's scalar path (oracle port) over jobs grouped by (kind, n):
+    groups maps (kind, n) -> host input array (rows = transforms).  Every host
+    thread runs its own share of each group; repeated until min_seconds."""
+    import numpy as np
+    from oracle import oracle as orc
+
+    orc.build(with_reference=False)
+    threads = os.cpu_count() or 1
+    o = orc.Oracle(max(n for _, n in groups), fast=True)
+    outs = {}
+    for (kind, n), xs in groups.items():
+        rows = xs.shape[0]
+        outs[(kind, n)] = (np.empty((rows, n // 2 + 1), np.complex64) if kind == "rfwd"
+                           else np.empty((rows, n), np.float32) if kind == "rinv"
+                           else np.empty((rows, n), np.complex64))
+    from ckfft_gb300 import workloads as wl
+
+    algo = sum(xs.shape[0] * wl.algorithmic_bytes(kind in ("rfwd", "rinv"), n) for (kind, n), xs in groups.items())
+    count = sum(xs.shape[0] for xs in groups.values())
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        for (kind, n), xs in groups.items():
+            o.batch_into(ORACLE_KIND[kind], n, xs.shape[0], xs, outs[(kind, n)], threads)
+        reps += 1
+        if time.perf_counter() - t0 >= min_seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": round(reps * algo / dt / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "transforms_per_s": round(reps * count / dt, 1), "reps": reps, "seconds": round(dt, 3)}
+
+
+def measure_w4(args):
+    """Workload 4: 10000 transforms of uneven sizes in one graph replay (the persistent job
+    kernel plus grouped launches over pointer tables), against the plain path of one CkFft*
+    call per transform and against the reference's scalar path on the host cores."""
+    import numpy as np
+    import torch
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+
+    ctx = binding.Context(1 << 16)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(wl.W4_SEED)
+    jobs = w4_jobs(torch, g)
     plan = ctx.plan(jobs)
     stream = torch.cuda.Stream()
     for _ in range(max(args.warmup, 3)):
         ctx.check(plan.exec(stream))
     torch.cuda.synchronize()
+    # gate: every job of two sizes (complex 2^16 forward, real 2^16 inverse) and a
+    # spread of others against the oracle
+    gate = w4_gate(jobs)
     launches0 = binding.launch_count()
     secs = timed_steps(torch, stream, lambda: ctx.check(plan.exec(stream)), args.steps)
     launches = binding.launch_count() - launches0
     value = args.steps * plan.bytes / secs / 1e9
     tps = args.steps * len(jobs) / secs
-    # the plain path: one blocking drop-in call per transform (device pointers)
     tmp = torch.empty((1 << 15) + 1, dtype=torch.complex64, device="cuda")
+
     def per_call():
         for kind, n, _, x, y in jobs:
             if kind == "cfwd":
@@ -691,102 +783,310 @@ def run_w4(args):
         torch.cuda.synchronize()
         pc = time.perf_counter() - t0
     peak, src = measured_peaks()
-    line = base_line(args, "uneven batch FFT GB/s (10000 transforms, log2 n 6..16, mixed kinds)", value, "GB/s", secs,
-                     {"workload": "10000 transforms, log2 n uniform 6..16, 70% complex / 30% real, 50% inverse, "
-                                  "U[-1,1) inputs, one CUDA-graph replay per step (the persistent job kernel for "
-                                  "complex <= 2^12 / real <= 2^13, grouped launches over pointer tables above)",
-                      "jobs": len(jobs), "l2": f"{plan.bytes / 1e9:.2f} GB of algorithmic traffic per step (larger than L2)"})
-    line["transforms_per_s"] = round(tps, 1)
-    line["roofline"] = {"bound": "hbm", "kernel": "one graph: k_jobs + grouped k_l2_c2c / k_*_table launches",
-                        "achieved": round(value, 1), "peak": peak, "unit": "GB/s", "frac": round(value / peak, 4),
-                        "peak_source": src, "traffic": None,
-                        "note": "complex 2^15 / 2^16 (60% of the bytes) run the cluster two-pass kernel: one DRAM "
-                                "pass, two passes of instructions"}
+    out = {"metric": "uneven batch FFT GB/s (10000 transforms, log2 n 6..16, mixed kinds)",
+           "value": round(value, 2), "unit": "GB/s", "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4),
+           "frac_of_hbm": round(value / peak, 4), "peak": peak, "peak_source": src,
+           "transforms_per_s": round(tps, 1), "gpu_launches": launches, "oracle_gate": gate,
+           "config": {"workload": "10000 transforms, log2 n uniform 6..16, 70% complex / 30% real, 50% inverse, "
+                                  "U[-1,1) inputs, one CUDA-graph replay per step",
+                      "jobs": len(jobs), "bytes_per_step": plan.bytes,
+                      "l2": f"{plan.bytes / 1e9:.2f} GB of algorithmic traffic per step (larger than L2)"}}
     if pc is not None:
-        line["per_call"] = {"transforms_per_s": round(len(jobs) / pc, 1), "gbs": round(plan.bytes / pc / 1e9, 2),
-                            "api": "one CkFftComplex*/CkFftReal* call per transform (device pointers, blocking)",
-                            "speedup_of_persistent": round(tps / (len(jobs) / pc), 1)}
-    line["gpu_launches"] = launches
-    print(json.dumps(line), flush=True)
+        out["per_call"] = {"transforms_per_s": round(len(jobs) / pc, 1), "gbs": round(plan.bytes / pc / 1e9, 2),
+                           "api": "one CkFftComplex*/CkFftReal* call per transform (device pointers, blocking)",
+                           "speedup_of_plan": round(tps / (len(jobs) / pc), 1)}
+    if not args.no_cpu:
+        groups = {}
+        for kind, n, _, x, _ in jobs:
+            groups.setdefault((kind, n), []).append(x.cpu().numpy())
+        groups = {k: np.ascontiguousarray(np.stack(v)) for k, v in groups.items()}
+        cpu = time_cpu_jobs(groups)
+        cpu["sample"] = (f"all {len(jobs)} jobs of the batch (inputs copied to the host), grouped by kind and size, "
+                         f"repeated {cpu.pop('reps')} times in {cpu.pop('seconds')} s on {cpu['cores']} threads")
+        out["cpu_baseline"] = cpu
     plan.close()
     ctx.close()
+    return out
 
 
-def run_w5(args, nreq=600):
-    """Workload 5: Poisson request stream (sizes 2^k, k in 8..20, 1-64 frames,
-    mixed complex/real, N(0,1) inputs) at 10-90% of the server's measured peak,
-    through the continuous-batching server and through one call per request."""
+def w4_gate(jobs, per_group=4):
+    """A few transforms of every (kind, size) of the uneven batch against the oracle."""
+    from oracle import oracle as orc
+
+    orc.build(with_reference=False)
+    o = orc.Oracle(1 << 16)
+    seen, worst = {}, 0.0
+    for kind, n, _, x, y in jobs:
+        if seen.get((kind, n), 0) >= per_group:
+            continue
+        seen[(kind, n)] = seen.get((kind, n), 0) + 1
+        xh = x.cpu().numpy()
+        ref = (o.complex(n, xh, kind == "cinv") if kind in ("cfwd", "cinv")
+               else o.real_forward(n, xh) if kind == "rfwd" else o.real_inverse(n, xh))
+        e = orc.rel_l2(y.cpu().numpy(), ref)
+        if not e <= 1e-5:
+            raise SystemExit(f"w4 oracle gate: {kind} n={n} rel L2 {e:.3e}: refusing to report a number")
+        worst = max(worst, e)
+    return {"checked": sum(seen.values()), "groups": len(seen), "worst_rel_l2": worst}
+
+
+def run_w4(args):
+    out = measure_w4(args)
+    line = base_line(args, out["metric"], out["value"], "GB/s", out["ms_per_step"] * args.steps / 1e3, out["config"])
+    peak = out["peak"]
+    line["roofline"] = {"bound": "hbm", "kernel": "one graph: k_jobs + grouped launches over pointer tables",
+                        "achieved": out["value"], "peak": peak, "unit": "GB/s", "frac": out["frac_of_hbm"],
+                        "peak_source": out["peak_source"], "traffic": None}
+    for k in ("transforms_per_s", "per_call", "gpu_launches", "cpu_baseline", "oracle_gate"):
+        if k in out:
+            line[k] = out[k]
+    print(json.dumps(line), flush=True)
+
+
+def w5_requests(nreq, seed):
+    """(kind, n, frames) of the serving workload: 2^k points, k uniform in 8..20,
+    1-64 frames, complex / real and forward / inverse with equal odds."""
     import numpy as np
-    import torch
-    from ckfft_gb300 import binding
     from ckfft_gb300 import workloads as wl
 
-    rng = np.random.default_rng(wl.W5_SEED)
+    rng = np.random.default_rng(seed)
     lo, hi = wl.W5_LOG2
     l2 = rng.integers(lo, hi + 1, nreq)
     frames = rng.integers(1, 65, nreq)
     real = rng.uniform(size=nreq) < 0.5
     inv = rng.uniform(size=nreq) < 0.5
     kinds = [("rinv" if i else "rfwd") if r else ("cinv" if i else "cfwd") for r, i in zip(real, inv)]
-    ns = [1 << int(k) for k in l2]
+    return [(k, 1 << int(a), int(c)) for k, a, c in zip(kinds, l2, frames)]
 
-    def in_bytes(kind, n, c):
-        return c * (4 * n if kind == "rfwd" else 8 * (n // 2 + 1) if kind == "rinv" else 8 * n)
 
-    def out_bytes(kind, n, c):
-        return c * (8 * (n // 2 + 1) if kind == "rfwd" else 4 * n if kind == "rinv" else 8 * n)
+def io_bytes(kind, n, c):
+    fin = 4 * n if kind == "rfwd" else 8 * (n // 2 + 1) if kind == "rinv" else 8 * n
+    fout = 8 * (n // 2 + 1) if kind == "rfwd" else 4 * n if kind == "rinv" else 8 * n
+    return c * fin, c * fout
 
-    ctx = binding.Context(1 << hi)
-    max_in = max(in_bytes(k, n, int(c)) for k, n, c in zip(kinds, ns, frames))
-    g = torch.Generator(device="cuda")
-    g.manual_seed(wl.W5_SEED)
-    src = torch.randn(max_in // 4 + 16, generator=g, device="cuda")       # shared, read-only inputs
-    offs = np.cumsum([0] + [(out_bytes(k, n, int(c)) + 255) // 256 * 256 for k, n, c in zip(kinds, ns, frames)])
-    dst = torch.empty(int(offs[-1]) // 4 + 64, device="cuda")              # a distinct output per request
-    base_in, base_out = src.data_ptr(), dst.data_ptr()
-    reqs = [(k, n, int(c), base_in, base_out + int(o)) for k, n, c, o in zip(kinds, ns, frames, offs[:-1])]
-    algo = sum(wl.algorithmic_bytes(k in ("rfwd", "rinv"), n) * int(c) for k, n, c in zip(kinds, ns, frames))
-    mean_bytes = algo / nreq
 
-    srv = binding.Server(ctx, scratch_budget_bytes=4 << 30, max_inflight=2, direct_threshold_bytes=args.direct_mb << 20)
-    burst = [(0.0,) + r for r in reqs]
-    srv.replay(burst)                                                      # warm-up
-    ok, _, st = srv.replay(burst)
-    if not ok:
-        raise SystemExit(f"server replay failed: {binding.last_error()}")
-    peak_gbs = st["algo_bytes"] / st["seconds"] / 1e9
-    loads = []
-    for f in (0.1, 0.3, 0.5, 0.7, 0.9):
+def place(spec, in_base, in_cap, out_base, out_cap):
+    """Gives each request its own input and output window in two pools, in
+    order, wrapping to the start when a pool is used up (a pool is far larger
+    than L2, so no request finds its input in L2 from an earlier one)."""
+    reqs, oi, oo = [], 0, 0
+    for kind, n, c in spec:
+        bi, bo = io_bytes(kind, n, c)
+        bi, bo = (bi + 255) // 256 * 256, (bo + 255) // 256 * 256
+        if oi + bi > in_cap:
+            oi = 0
+        if oo + bo > out_cap:
+            oo = 0
+        reqs.append((kind, n, c, in_base + oi, out_base + oo))
+        oi += bi
+        oo += bo
+    return reqs
+
+
+def batched_peak(torch, ctx, reqs, host):
+    """GB/s of the request mix through the batched entry points, back to back:
+    device buffers asynchronously on one stream (CUDA events), host buffers
+    with the blocking staged calls (wall clock)."""
+    from ckfft_gb300 import workloads as wl
+
+    algo = sum(wl.algorithmic_bytes(k in ("rfwd", "rinv"), n) * c for k, n, c, _, _ in reqs)
+    if host:
+        for k, n, c, i, o in reqs[:8]:
+            ctx.check(ctx.batch(k, n, c, i, o))
+        t0 = time.perf_counter()
+        for k, n, c, i, o in reqs:
+            ctx.check(ctx.batch(k, n, c, i, o))
+        return algo / (time.perf_counter() - t0) / 1e9
+    stream = torch.cuda.Stream()
+
+    def step():
+        for k, n, c, i, o in reqs:
+            ctx.check(ctx.batch(k, n, c, i, o, stream))
+    step()
+    return algo / timed_steps(torch, stream, step, 1) / 1e9
+
+
+def w5_gate(srv, reqs, src, dst, count=24):
+    """The first requests (before any window wraps) through the server, the
+    first frame of each against the oracle.  src / dst: the pools (device or
+    page-locked host tensors) the requests' pointers point into."""
+    import numpy as np
+    from oracle import oracle as orc
+    from ckfft_gb300 import binding
+
+    orc.build(with_reference=False)
+    o = orc.Oracle(1 << 20)
+    import torch
+
+    sb, db = src.view(-1).view(torch.uint8), dst.view(-1).view(torch.uint8)
+    worst = 0.0
+    for k, n, c, i, out in reqs[:count]:
+        ok, _ = srv.wait(srv.submit(k, n, c, i, out), 60.0)
+        if not ok:
+            raise SystemExit(f"w5 gate: server request failed: {binding.last_error()}")
+        bi, bo = io_bytes(k, n, c)
+        oi, oo = i - src.data_ptr(), out - dst.data_ptr()
+        xin = sb[oi:oi + bi // c].cpu().numpy()
+        yout = db[oo:oo + bo // c].cpu().numpy()
+        if k in ("cfwd", "cinv"):
+            ref, got = o.complex(n, xin.view(np.complex64), k == "cinv"), yout.view(np.complex64)
+        elif k == "rfwd":
+            ref, got = o.real_forward(n, xin.view(np.float32)), yout.view(np.complex64)
+        else:
+            ref, got = o.real_inverse(n, xin.view(np.complex64)), yout.view(np.float32)
+        e = orc.rel_l2(got, ref)
+        if not e <= 1e-5:
+            raise SystemExit(f"w5 gate: {k} n={n} rel L2 {e:.3e}: refusing to report a number")
+        worst = max(worst, e)
+    return {"checked": min(count, len(reqs)), "worst_rel_l2": worst}
+
+
+def serve_sweep(torch, ctx, srv, reqs, peak_gbs, loads, seed):
+    """Poisson arrivals at each offered load (fraction of peak_gbs): the server
+    replay and the one-call-per-request replay of the same trace."""
+    import numpy as np
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+
+    mean_bytes = sum(wl.algorithmic_bytes(k in ("rfwd", "rinv"), n) * c for k, n, c, _, _ in reqs) / len(reqs)
+    rows = []
+    for f in loads:
         rate = f * peak_gbs * 1e9 / mean_bytes
-        t = np.cumsum(np.random.default_rng(int(f * 100)).exponential(1.0 / rate, nreq))
+        t = np.cumsum(np.random.default_rng(seed + int(f * 100)).exponential(1.0 / rate, len(reqs)))
+        t -= t[0]
         trace = [(float(ti),) + r for ti, r in zip(t, reqs)]
         ok1, _, s1 = srv.replay(trace)
         ok2, _, s2 = binding.replay_per_request(ctx, trace)
         if not (ok1 and ok2):
             raise SystemExit(f"replay failed: {binding.last_error()}")
-        row = {"load": f, "offered_req_per_s": round(rate, 1)}
+        row = {"load": f, "offered_req_per_s": round(rate, 1), "offered_gbs": round(f * peak_gbs, 1)}
         for name, sx in (("server", s1), ("per_request", s2)):
             row[name] = {"p50_ms": round(sx["p50_s"] * 1e3, 4), "p99_ms": round(sx["p99_s"] * 1e3, 4),
                          "p999_ms": round(sx["p999_s"] * 1e3, 4), "max_ms": round(sx["max_s"] * 1e3, 4),
                          "throughput_gbs": round(sx["algo_bytes"] / sx["seconds"] / 1e9, 1)}
-        loads.append(row)
+        rows.append(row)
+    return rows
+
+
+def time_cpu_requests(spec, min_seconds=2.0):
+    """The reference's scalar path (oracle port) on requests of the serving mix,
+    taken in order until min_seconds of work: GB/s over those requests."""
+    import numpy as np
+    from oracle import oracle as orc
+    from ckfft_gb300 import workloads as wl
+
+    orc.build(with_reference=False)
+    threads = os.cpu_count() or 1
+    o = orc.Oracle(1 << 20, fast=True)
+    rng = np.random.default_rng(1)
+    done_b, done_r, t_work = 0, 0, 0.0
+    for kind, n, c in spec:
+        if kind == "rfwd":
+            x = rng.standard_normal((c, n), dtype=np.float32)
+            y = np.empty((c, n // 2 + 1), np.complex64)
+        elif kind == "rinv":
+            x = (rng.standard_normal((c, n // 2 + 1)) + 1j * rng.standard_normal((c, n // 2 + 1))).astype(np.complex64)
+            y = np.empty((c, n), np.float32)
+        else:
+            x = (rng.standard_normal((c, n)) + 1j * rng.standard_normal((c, n))).astype(np.complex64)
+            y = np.empty((c, n), np.complex64)
+        t0 = time.perf_counter()
+        o.batch_into(ORACLE_KIND[kind], n, c, x, y, threads)
+        t_work += time.perf_counter() - t0
+        done_b += wl.algorithmic_bytes(kind in ("rfwd", "rinv"), n) * c
+        done_r += 1
+        if t_work >= min_seconds:
+            break
+    return {"value": round(done_b / t_work / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "requests_per_s": round(done_r / t_work, 1),
+            "sample": f"the first {done_r} requests of the serving mix (N(0,1) inputs), {t_work:.2f} s of transform "
+                      f"time on {threads} threads, each request's frames spread over the threads"}
+
+
+def measure_w5(args, loads=(0.1, 0.3, 0.5, 0.7, 0.9), host_requests=2000):
+    """Workload 5: Poisson request streams (2^k points, k in 8..20, 1-64 frames,
+    mixed complex/real, N(0,1) inputs) at 10-90% of the peak offered load,
+    through the continuous-batching server and through one call per request.
+    Peak offered load = the batched throughput of the same request mix through
+    CkFftCuda*Batch.  Every request reads its own input window and writes its
+    own output window of pools far larger than L2.  Device-resident requests
+    at every load; page-locked host requests (staged by the server, every byte
+    crossing the CPU-GPU link inside the latency) at 50%."""
+    import torch
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+
+    nreq = args.requests
+    spec = w5_requests(nreq, wl.W5_SEED)
+    ctx = binding.Context(1 << wl.W5_LOG2[1])
+    g = torch.Generator(device="cuda")
+    g.manual_seed(wl.W5_SEED)
+    pool_b = 8 << 30
+    src = torch.randn(pool_b // 4, generator=g, device="cuda")
+    dst = torch.empty(pool_b // 4, device="cuda")
+    reqs = place(spec, src.data_ptr(), pool_b, dst.data_ptr(), pool_b)
+    algo = sum(wl.algorithmic_bytes(k in ("rfwd", "rinv"), n) * c for k, n, c in spec)
+    srv = binding.Server(ctx, scratch_budget_bytes=4 << 30, max_inflight=2, direct_threshold_bytes=args.direct_mb << 20)
+    gate = w5_gate(srv, reqs, src, dst)
+    peak = batched_peak(torch, ctx, reqs, host=False)
+    srv.replay([(0.0,) + r for r in reqs[:200]])                         # warm-up
+    rows = serve_sweep(torch, ctx, srv, reqs, peak, loads, 100)
     srv.close()
-    mid = next(r for r in loads if r["load"] == 0.5)
-    line = {"metric": "served p99 latency at 50% of peak offered load", "value": mid["server"]["p99_ms"],
-            "unit": "ms", "n_gpus": 1, "steps": len(loads), "warmup": 1, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded N(0,1) inputs)",
-            "config": {"workload": f"{nreq} requests, size 2^k with k uniform in {lo}..{hi}, 1-64 frames, "
-                                   "50% real / 50% complex, 50% inverse, Poisson arrivals",
-                       "server": f"2 job-kernel runs in flight, requests >= {args.direct_mb} MiB on 2 direct lanes, "
-                                 "4 GiB scratch budget, device-resident inputs and outputs",
-                       "mean_request_mb": round(mean_bytes / 1e6, 2)},
-            "peak_gbs": round(peak_gbs, 1), "loads": loads}
-    print(json.dumps(line), flush=True)
+    # page-locked host requests at 50% of their own batched peak
+    hb = 4 << 30
+    hsrc = torch.empty(hb // 4).pin_memory()
+    hsrc.copy_(src[: hb // 4])
+    hdst = torch.empty(hb // 4).pin_memory()
+    del src, dst
+    torch.cuda.empty_cache()
+    hspec = spec[:host_requests]
+    hreqs = place(hspec, hsrc.data_ptr(), hb, hdst.data_ptr(), hb)
+    srv = binding.Server(ctx, scratch_budget_bytes=4 << 30, max_inflight=2, direct_threshold_bytes=args.direct_mb << 20)
+    hgate = w5_gate(srv, hreqs, hsrc, hdst, count=8)
+    hpeak = batched_peak(torch, ctx, hreqs, host=True)
+    srv.replay([(0.0,) + r for r in hreqs[:50]])
+    hrows = serve_sweep(torch, ctx, srv, hreqs, hpeak, (0.5,), 200)
+    srv.close()
     ctx.close()
+    mid = next(r for r in rows if r["load"] == 0.5)
+    out = {"metric": "served p99 latency at 50% of peak offered load", "value": mid["server"]["p99_ms"], "unit": "ms",
+           "higher_is_better": False, "peak_gbs": round(peak, 1), "peak_definition":
+               "batched throughput of the same request mix through CkFftCuda*Batch (device buffers, back to back)",
+           "mean_request_mb": round(algo / nreq / 1e6, 2), "requests_per_load": nreq, "loads": rows,
+           "oracle_gate": gate,
+           "host_resident": {"requests": len(hreqs), "peak_gbs": round(hpeak, 1), "loads": hrows, "oracle_gate": hgate,
+                             "peak_definition": "batched throughput of the same mix through CkFftCuda*Batch from "
+                                                "page-locked host buffers (blocking, staged over the CPU-GPU link)"},
+           "config": {"workload": f"{nreq} requests per load, size 2^k with k uniform in {wl.W5_LOG2[0]}..{wl.W5_LOG2[1]}, "
+                                  "1-64 frames, 50% real / 50% complex, 50% inverse, N(0,1) inputs, Poisson arrivals",
+                      "server": f"2 job-kernel runs in flight, requests >= {args.direct_mb} MiB on 2 direct lanes, "
+                                "4 GiB scratch budget",
+                      "inputs": "each request reads its own window of an 8 GiB pool (device) / 4 GiB pool (host), "
+                                "wrapping only after the pool is used up"}}
+    if not args.no_cpu:
+        out["cpu_baseline"] = time_cpu_requests(spec)
+    return out
+
+
+def run_w5(args):
+    out = measure_w5(args)
+    line = {"metric": out["metric"], "value": out["value"], "unit": "ms", "n_gpus": 1, "steps": len(out["loads"]),
+            "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded N(0,1) inputs)", "config": out["config"]}
+    for k in ("peak_gbs", "peak_definition", "mean_request_mb", "requests_per_load", "loads", "host_resident",
+              "oracle_gate", "cpu_baseline"):
+        if k in out:
+            line[k] = out[k]
+    print(json.dumps(line), flush=True)
 
 
 def main():
     args = parse_args()
+    world_env = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus != world_env:
+        sys.stderr.write(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world_env}; launch one rank per GPU with "
+                         f"`python -m torch.distributed.run --nproc-per-node {args.gpus} bench.py --gpus {args.gpus}`\n")
+        raise SystemExit(2)
     if args.workload != "w2" and args.impl == "ours":
         {"w1": run_w1, "w3": run_w3, "w4": run_w4, "w5": run_w5, "sizes": run_sizes}[args.workload](args)
         return

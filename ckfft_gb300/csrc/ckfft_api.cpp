@@ -345,6 +345,8 @@ size_t scratch_need(const Work& w, long long cnt)
 {
     if (!needs_large(w)) return 0;
     if (!is_real(w.kind) && ckg::cluster_supported(w.log2n) && ckg::cluster_enabled()) return 0;
+    if (!is_real(w.kind) && ckg::mid_supported(w.log2n) && ckg::mid_enabled())
+        return ckg::mid_scratch_bytes(w.log2n, cnt);
     const size_t one = ckg::large_scratch_bytes(w.kind, w.log2n);
     const size_t cap = 256ull << 20;
     long long g = (long long)(cap / one);

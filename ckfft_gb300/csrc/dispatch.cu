@@ -21,6 +21,8 @@ cudaError_t prepare_fused();
 cudaError_t prepare_inter();
 cudaError_t prepare_l2pass();
 cudaError_t prepare_groups();
+cudaError_t prepare_noalloc();
+cudaError_t prepare_mid();
 
 // Opt-in (CKFFT_CUDA_CLUSTER=1): measured slower than the default paths on
 // GB300 (2^14: 2366 vs 3669 GB/s single CTA; 2^15 / 2^16: 1936 / 1516 vs about
@@ -30,6 +32,17 @@ bool cluster_enabled()
 {
     static const bool on = [] {
         const char* v = std::getenv("CKFFT_CUDA_CLUSTER");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
+// Off unless CKFFT_CUDA_MID=1 (otherwise the cluster two-pass kernel of
+// fft_l2pass.cu runs complex 2^15 / 2^16).
+bool mid_enabled()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("CKFFT_CUDA_MID");
         return v && v[0] == '1';
     }();
     return on;
@@ -196,6 +209,8 @@ cudaError_t prepare_device()
     if ((e = prepare_inter()) != cudaSuccess) return e;
     if ((e = prepare_l2pass()) != cudaSuccess) return e;
     if ((e = prepare_groups()) != cudaSuccess) return e;
+    if ((e = prepare_noalloc()) != cudaSuccess) return e;
+    if ((e = prepare_mid()) != cudaSuccess) return e;
     if (dev < 64) done |= 1ull << dev;
     return cudaSuccess;
 }

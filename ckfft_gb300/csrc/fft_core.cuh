@@ -199,12 +199,20 @@ __host__ __device__ constexpr bool is_padded()
     else return false;
 }
 
-// Barrier covering every thread that shares the view (warp or block).
-template <bool WARP>
+// Barrier covering every thread that shares the view: the warp, the block,
+// or (BAR_ID > 0) the BAR_N threads of a named barrier -- a group of warps
+// inside a block whose other warps do other work.
+template <bool WARP, int BAR_ID = 0, int BAR_N = 0>
 __device__ __forceinline__ void xsync()
 {
-    if constexpr (WARP) __syncwarp();
-    else __syncthreads();
+    if constexpr (WARP) {
+        __syncwarp();
+    } else if constexpr (BAR_ID > 0) {
+        static_assert(BAR_N > 0 && BAR_N % 32 == 0, "a named barrier counts whole warps");
+        asm volatile("bar.sync %0, %1;" ::"n"(BAR_ID), "n"(BAR_N) : "memory");
+    } else {
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------- programmatic dependent launch
@@ -271,7 +279,7 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[1 << LOG2R], int t, co
 
 // Writes a stage's outputs to their Stockham positions, then reloads the
 // thread's registers with positions t + m*T.
-template <int LOG2N, int LOG2R, int LRS, int LNS, bool WARP, class View>
+template <int LOG2N, int LOG2R, int LRS, int LNS, bool WARP, int BAR_ID = 0, int BAR_N = 0, class View>
 __device__ __forceinline__ void stage_exchange(float2 (&v)[1 << LOG2R], int t, const View& view)
 {
     constexpr int R = 1 << LOG2R, RS = 1 << LRS, NS = 1 << LNS;
@@ -298,7 +306,7 @@ __device__ __forceinline__ void stage_exchange(float2 (&v)[1 << LOG2R], int t, c
             for (int j = 0; j < RS; ++j) view.st(base + j * NS, v[u + j * U]);
         }
     }
-    xsync<WARP>();
+    xsync<WARP, BAR_ID, BAR_N>();
     if constexpr (kFastRead) {
         const float2* q = view.base + PaddedView::pad(t);
 #pragma unroll
@@ -307,13 +315,14 @@ __device__ __forceinline__ void stage_exchange(float2 (&v)[1 << LOG2R], int t, c
 #pragma unroll
         for (int m = 0; m < R; ++m) v[m] = view.ld(t + m * T);
     }
-    xsync<WARP>();
+    xsync<WARP, BAR_ID, BAR_N>();
 }
 
 // Full transform of one length-2^LOG2N sequence held as v[m] = x[t + m*T].
 // On return v[m] = X[t + m*T].  The view must not be in use by other code
 // between the call's barriers.
-template <int LOG2N, int LOG2R, bool INV, bool WARP, class View>
+// BAR_ID > 0: the threads sharing the view meet at that named barrier (BAR_N threads).
+template <int LOG2N, int LOG2R, bool INV, bool WARP, int BAR_ID = 0, int BAR_N = 0, class View>
 __device__ __forceinline__ void stockham(float2 (&v)[1 << LOG2R], int t, const float2* __restrict__ tw, const View& view)
 {
     if constexpr (LOG2N == 0) {
@@ -325,7 +334,7 @@ __device__ __forceinline__ void stockham(float2 (&v)[1 << LOG2R], int t, const f
             constexpr int lrs = S::lrs(s), lns = S::lns(s);
             stage_compute<LOG2N, LOG2R, lrs, lns, INV>(v, t, tw);
             if constexpr (s + 1 < S::nstages)
-                stage_exchange<LOG2N, LOG2R, lrs, lns, WARP>(v, t, view);
+                stage_exchange<LOG2N, LOG2R, lrs, lns, WARP, BAR_ID, BAR_N>(v, t, view);
         });
     }
 }

@@ -65,6 +65,8 @@ cudaError_t launch_group(int op, int log2a, const FrameDesc* fr, long long count
                          void* scratch, size_t scratch_bytes, cudaStream_t s);
 cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
                                 void* scratch, size_t scratch_bytes, cudaStream_t s);
+cudaError_t launch_mid_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
+                             void* scratch, size_t scratch_bytes, cudaStream_t s);
 cudaError_t launch_r2c_table(int lm, const FrameDesc* fr, long long count, const float2* tw, void* scratch,
                              size_t scratch_bytes, cudaStream_t s);
 cudaError_t launch_c2r_table(int lm, const FrameDesc* fr, long long count, const float2* tw, void* scratch,
@@ -132,9 +134,14 @@ void free_run_slot(RunSlot* r);
 // NULL uses (and grows) the slot's own scratch.
 int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunSlot* r, cudaStream_t s,
                 float2* scratch_override = nullptr);
-bool validate_job(const ContextView& cv, const CkFftCudaJob& j, int index);
+bool validate_job(const ContextView& cv, const CkFftCudaJob& j, int index, bool allow_host = false);
 long long job_scratch_bytes(const CkFftCudaJob& j);
 long long job_algo_bytes(const CkFftCudaJob& j);
+// Bytes of a job's whole input / output; whether a buffer is outside the
+// context's device (host memory, to be staged).
+long long job_in_bytes(const CkFftCudaJob& j);
+long long job_out_bytes(const CkFftCudaJob& j);
+bool job_host_side(const ContextView& cv, const void* p);
 
 // Launches the job kernel on all resident CTAs of the current device.
 cudaError_t launch_jobs(const JobsArgs& a, cudaStream_t s);

@@ -106,9 +106,22 @@ static bool on_device(const void* p, int dev)
     return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
+// Host memory (page-locked or pageable) as cudaPointerGetAttributes reports it.
+static bool on_host(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeUnregistered;
+}
+
 // Checks one job against the rules of the single calls plus the job
 // kernel's limits; sets the error message (naming job `j`) on failure.
-bool validate_job(const ContextView& cv, const CkFftCudaJob& J, int j)
+// allow_host: the buffers may also be host memory (the request server stages
+// such requests through its own device buffers).
+bool validate_job(const ContextView& cv, const CkFftCudaJob& J, int j, bool allow_host)
 {
     char msg[200];
     if (J.kind < 0 || J.kind > 3) {
@@ -139,8 +152,10 @@ bool validate_job(const ContextView& cv, const CkFftCudaJob& J, int j)
         set_last_error(msg);
         return false;
     }
-    if (!on_device(J.input, cv.device) || !on_device(J.output, cv.device)) {
-        snprintf(msg, sizeof msg, "job %d: jobs take device (or managed) memory", j);
+    if (!((on_device(J.input, cv.device) || (allow_host && on_host(J.input))) &&
+          (on_device(J.output, cv.device) || (allow_host && on_host(J.output))))) {
+        snprintf(msg, sizeof msg, allow_host ? "job %d: buffers must be host memory or device memory of the context's device"
+                                             : "job %d: jobs take device (or managed) memory", j);
         set_last_error(msg);
         return false;
     }
@@ -329,6 +344,20 @@ long long job_scratch_bytes(const CkFftCudaJob& j)
     const int lc = ilog2ll(j.n) - (real ? 1 : 0);
     if ((real && j.n <= 4) || lc <= kJobMaxSingleLog2) return 0;
     return (long long)j.count * (long long)sizeof(float2) * (1ll << lc);
+}
+
+bool job_host_side(const ContextView& cv, const void* p) { return !on_device(p, cv.device); }
+
+long long job_in_bytes(const CkFftCudaJob& j)
+{
+    const bool real = j.kind >= 2, inverse = j.kind == 1 || j.kind == 3;
+    return (long long)j.count * (real ? (inverse ? 8ll * (j.n / 2 + 1) : 4ll * j.n) : 8ll * j.n);
+}
+
+long long job_out_bytes(const CkFftCudaJob& j)
+{
+    const bool real = j.kind >= 2, inverse = j.kind == 1 || j.kind == 3;
+    return (long long)j.count * (real ? (inverse ? 4ll * j.n : 8ll * (j.n / 2 + 1)) : 8ll * j.n);
 }
 
 long long job_algo_bytes(const CkFftCudaJob& j)

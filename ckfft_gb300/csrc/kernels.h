@@ -114,6 +114,17 @@ cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long l
                           long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes,
                           cudaStream_t stream);
 
+// Complex 2^15 and 2^16 on persistent CTAs, one transform per CTA at a time,
+// both passes inside the CTA with bulk-copied tiles and the intermediate in
+// L2 (fft_mid.cu).  scratch: mid_scratch_bytes(), 128-byte aligned; in
+// 16-byte aligned, in_dist even.  kind 0 / 1: forward / inverse.
+// mid_enabled(): only with CKFFT_CUDA_MID=1.
+bool mid_supported(int log2n);
+bool mid_enabled();
+size_t mid_scratch_bytes(int log2n, long long count);
+cudaError_t launch_mid(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,
+                       long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes, cudaStream_t stream);
+
 // Scratch bytes one transform of the given kind and size needs on the large path.
 size_t large_scratch_bytes(Kind kind, int log2n);
 

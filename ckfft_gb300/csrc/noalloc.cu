@@ -19,9 +19,15 @@
 //     on it; callers must order such calls themselves;
 //   * the array keeps the last call's contents; nothing in it has to start
 //     at zero (pass 1 overwrites every element pass 2 reads).
-// The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress while that device is current; that first call should
-// come before any stream capture begins.
+// The array's device address is looked up with cudaGetSymbolAddress (the
+// host-side name is only a stand-in, never a device address) once per device,
+// with that device current, when the first context is created on it
+// (prepare_noalloc, called from the per-device set-up of CkFftInit).  That
+// look-up loads this file's module, so the 8 MiB is committed at context
+// creation and the entry point itself only reads the cached pointer.  A
+// cudaDeviceReset destroys the array with everything else on the device:
+// after one, unload the library (or restart the process) before using it
+// again, since the cached addresses would be stale.
 #include <mutex>
 
 #include "ckfft_cuda.h"
@@ -45,17 +51,12 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 void* g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (set-up on first use).
+// Device address of g_noalloc_scratch on `dev`, resolved by prepare_noalloc.
 cudaError_t scratch_address(int dev, void** ptr)
 {
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_addr[dev] = p;
-    }
+    if (!g_scratch_addr[dev]) return cudaErrorNotReady;      // no context was created on dev
     *ptr = g_scratch_addr[dev];
     return cudaSuccess;
 }
@@ -78,6 +79,26 @@ bool on_device(const void* p, int dev)
 }
 
 }  // namespace
+
+namespace ckg {
+
+// Resolves the array's device address on the current device (idempotent).
+cudaError_t prepare_noalloc()
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    if (g_scratch_addr[dev]) return cudaSuccess;
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_addr[dev] = p;
+    return cudaSuccess;
+}
+
+}  // namespace ckg
 
 extern "C" int CkFftCudaComplexBatchNoAlloc(CkFftContext* context, int n, int count, int inverse,
                                             const CkFftComplex* input, CkFftComplex* output, void* stream)

@@ -1,6 +1,6 @@
 // server.cpp -- continuous-batching request server over the persistent job kernel.
 //
-// Clients submit jobs (device buffers) at any time; a dispatcher thread owns
+// Clients submit jobs (device or host buffers) at any time; a dispatcher thread owns
 // the GPU side.  It keeps up to `max_inflight` runs on the device at once,
 // each on its own stream with resident descriptor buffers, pinned staging and
 // a scratch arena.  Whenever a run slot is free and requests are waiting it
@@ -14,9 +14,14 @@
 // `direct_threshold_bytes` already fill the GPU on their own: they skip
 // batching and go to one of two direct lanes (the batched entry points on a
 // lane stream), so a small request never waits behind a large one inside a
-// run.  Completion is detected by polling each run's or lane's event; latency
-// is measured from submission (or scheduled arrival, for trace replays) to
-// the dispatcher observing the completion.
+// run.  Requests may hold host buffers: their inputs are copied into a
+// device staging buffer owned by the run slot (or lane) on that slot's
+// stream before the kernels, and their outputs copied back after them, so
+// the copies of one run overlap the kernels of the others; the staging
+// buffers grow to the largest run seen and then stay resident.  Completion
+// is detected by polling each run's or lane's event (recorded after the
+// output copies); latency is measured from submission (or scheduled arrival,
+// for trace replays) to the dispatcher observing the completion.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -43,7 +48,11 @@ double seconds_between(Clock::time_point a, Clock::time_point b)
 }
 
 struct Request {
-    CkFftCudaJob job;
+    CkFftCudaJob job;           // as submitted
+    bool host_in = false;       // input / output outside the device: staged
+    bool host_out = false;
+    long long in_bytes = 0;
+    long long out_bytes = 0;
     long long ticket;
     Clock::time_point t0;       // submission or scheduled arrival
     long long scratch;          // bytes of multi-pass intermediates
@@ -56,8 +65,15 @@ struct Result {
     double latency = 0.0;
 };
 
+// Device staging for the host-side buffers of the requests in one run.
+struct Stage {
+    void* buf = nullptr;
+    size_t cap = 0;
+};
+
 struct Slot {
     ckg::RunSlot run;
+    Stage stage;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev = nullptr;
     bool busy = false;
@@ -68,6 +84,7 @@ struct Slot {
 // A direct lane runs one large request at a time through the batched entry
 // points (one launch, or two or three for multi-pass sizes) on its own stream.
 struct Lane {
+    Stage stage;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev = nullptr;
     bool busy = false;
@@ -76,6 +93,61 @@ struct Lane {
 
 constexpr int kMaxRequestsPerRun = 4096;
 constexpr int kDirectLanes = 2;
+// Staged (host-side) bytes one run admits; a single larger request runs alone.
+constexpr long long kStageBytesPerRun = 1ll << 30;
+
+long long staged_bytes(const Request& r)
+{
+    auto up = [](long long b) { return (b + 255) / 256 * 256; };
+    return (r.host_in ? up(r.in_bytes) : 0) + (r.host_out ? up(r.out_bytes) : 0);
+}
+
+// Copies the host-side inputs of `reqs` into the stage on `st` and points the
+// jobs at the staged copies (inputs and outputs).  The stage grows when
+// needed; the caller's stream is idle then (the slot or lane is free).
+cudaError_t stage_inputs(const std::vector<Request>& reqs, std::vector<CkFftCudaJob>& jobs, Stage* stage,
+                         cudaStream_t st)
+{
+    size_t need = 0;
+    for (const Request& r : reqs) need += (size_t)staged_bytes(r);
+    if (need == 0) return cudaSuccess;
+    if (need > stage->cap) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        cudaFree(stage->buf);
+        stage->buf = nullptr;
+        stage->cap = 0;
+        if ((e = ckg::dev_malloc(&stage->buf, need)) != cudaSuccess) return e;
+        stage->cap = need;
+    }
+    char* p = (char*)stage->buf;
+    for (size_t i = 0; i < reqs.size(); ++i) {
+        const Request& r = reqs[i];
+        if (r.host_in) {
+            cudaError_t e = cudaMemcpyAsync(p, r.job.input, (size_t)r.in_bytes, cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) return e;
+            jobs[i].input = p;
+            p += (r.in_bytes + 255) / 256 * 256;
+        }
+        if (r.host_out) {
+            jobs[i].output = p;
+            p += (r.out_bytes + 255) / 256 * 256;
+        }
+    }
+    return cudaSuccess;
+}
+
+// Copies the staged outputs back to the requests' host buffers on `st`.
+cudaError_t stage_outputs(const std::vector<Request>& reqs, const std::vector<CkFftCudaJob>& jobs, cudaStream_t st)
+{
+    for (size_t i = 0; i < reqs.size(); ++i) {
+        const Request& r = reqs[i];
+        if (!r.host_out) continue;
+        cudaError_t e = cudaMemcpyAsync(r.job.output, jobs[i].output, (size_t)r.out_bytes, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
 
 }  // namespace
 
@@ -171,9 +243,10 @@ std::vector<Request> admit(CkFftCudaServer* s, bool* oversized)
 {
     std::vector<Request> out;
     *oversized = false;
-    long long scratch = 0;
+    long long scratch = 0, staged = 0;
     while (!s->pending.empty() && (int)out.size() < kMaxRequestsPerRun) {
         const Request& r = s->pending.front();
+        if (!out.empty() && staged + staged_bytes(r) > kStageBytesPerRun) break;
         if (scratch + r.scratch > (long long)s->arena) {
             if (!out.empty()) break;
             // alone and larger than an arena: admit if free HBM covers it
@@ -185,6 +258,7 @@ std::vector<Request> admit(CkFftCudaServer* s, bool* oversized)
             break;
         }
         scratch += r.scratch;
+        staged += staged_bytes(r);
         out.push_back(r);
         s->pending.pop_front();
     }
@@ -219,7 +293,9 @@ void dispatch_loop(CkFftCudaServer* s)
                 s->direct.pop_front();
             }
             ln.reqs.assign(1, r);
-            if (enqueue_direct(s, r.job, ln.stream) && cudaEventRecord(ln.ev, ln.stream) == cudaSuccess) {
+            std::vector<CkFftCudaJob> one(1, r.job);
+            if (stage_inputs(ln.reqs, one, &ln.stage, ln.stream) == cudaSuccess && enqueue_direct(s, one[0], ln.stream) &&
+                stage_outputs(ln.reqs, one, ln.stream) == cudaSuccess && cudaEventRecord(ln.ev, ln.stream) == cudaSuccess) {
                 ln.busy = true;
                 ++busy;
             } else {
@@ -265,8 +341,10 @@ void dispatch_loop(CkFftCudaServer* s)
             } else if (scratch) {
                 override_scratch = sl.run.scratch;
             }
+            ok = ok && stage_inputs(sl.reqs, jobs, &sl.stage, sl.stream) == cudaSuccess;
             const int rc = ok ? ckg::enqueue_run(s->cv, jobs.data(), (int)jobs.size(), &sl.run, sl.stream, override_scratch) : -1;
-            if (rc == 1 && cudaEventRecord(sl.ev, sl.stream) == cudaSuccess) {
+            if (rc == 1 && stage_outputs(sl.reqs, jobs, sl.stream) == cudaSuccess &&
+                cudaEventRecord(sl.ev, sl.stream) == cudaSuccess) {
                 sl.busy = true;
                 ++busy;
             } else {
@@ -292,9 +370,15 @@ void dispatch_loop(CkFftCudaServer* s)
 
 long long submit(CkFftCudaServer* s, const CkFftCudaJob& job, Clock::time_point t0)
 {
-    if (!ckg::validate_job(s->cv, job, 0)) return 0;
+    if (!ckg::validate_job(s->cv, job, 0, true)) return 0;
     Request r;
     r.job = job;
+    if (job.count > 0) {
+        r.host_in = ckg::job_host_side(s->cv, job.input);
+        r.host_out = ckg::job_host_side(s->cv, job.output);
+        r.in_bytes = ckg::job_in_bytes(job);
+        r.out_bytes = ckg::job_out_bytes(job);
+    }
     r.t0 = t0;
     r.scratch = ckg::job_scratch_bytes(job);
     r.bytes = ckg::job_algo_bytes(job);
@@ -418,11 +502,13 @@ void CkFftCudaServerDestroy(CkFftCudaServer* s)
     for (Slot& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         ckg::free_run_slot(&sl.run);
+        cudaFree(sl.stage.buf);
         if (sl.ev) cudaEventDestroy(sl.ev);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
     for (Lane& ln : s->lanes) {
         if (ln.stream) cudaStreamSynchronize(ln.stream);
+        cudaFree(ln.stage.buf);
         if (ln.ev) cudaEventDestroy(ln.ev);
         if (ln.stream) cudaStreamDestroy(ln.stream);
     }

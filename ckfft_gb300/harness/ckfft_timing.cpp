@@ -7,13 +7,13 @@
 // per tester, and records the median milliseconds per transform in
 // results_linux_<machine>.xml in the reference's layout:
 //
-//   <ckfft_test><fft_4096><ckfft time="..." /><kiss_fft time="..." />...</fft_4096>...</ckfft_test>
+//   <ckfft_test><fft_4096><ckfft time="..." /><ckfft_kiss_api time="..." />...</fft_4096>...</ckfft_test>
 //
 // Testers (one transform per call unless noted):
 //   ckfft         the reference-named calls on host (pageable) buffers, the
 //                 reference harness's usage (src/test/test.cpp:269-297);
 //   ckfft_device  the same calls on device buffers;
-//   kiss_fft      the kiss_fft-compatible calls of this library on host
+//   ckfft_kiss_api the kiss_fft-compatible calls of this library on host
 //                 buffers (the reference harness's second tester,
 //                 src/test/test.cpp:315-395);
 //   ckfft_batch   CkFftCuda*Batch of 4096 transforms on device buffers,
@@ -185,7 +185,7 @@ struct Kiss : Tester {
     CkFftComplex* out = nullptr;
     int n = 0;
     bool inv = false, real = false;
-    const char* name() const override { return "kiss_fft"; }
+    const char* name() const override { return "ckfft_kiss_api"; }
     void init(const CkFftComplex* i, CkFftComplex* o, int count, bool inverse, bool r) override
     {
         out = o, n = count, inv = inverse, real = r;

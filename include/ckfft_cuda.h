@@ -284,8 +284,13 @@ CkFftCudaServer* CkFftCudaServerCreate(CkFftContext* context, size_t scratch_bud
                                        long long direct_threshold_bytes);
 void CkFftCudaServerDestroy(CkFftCudaServer* server);   /* finishes admitted work first */
 
-/* Queues one request (validated like a job; device buffers).  Returns a ticket
- * > 0, or 0 on error.  Never blocks on the GPU. */
+/* Queues one request (validated like a job).  Its buffers may be device
+ * memory of the context's device or host memory: host-side inputs are copied
+ * into the server's resident device staging buffers on the run's stream, and
+ * outputs copied back before the request completes (page-locked host memory
+ * keeps those copies asynchronous; pageable memory works but makes the
+ * dispatcher wait for each copy).  Returns a ticket > 0, or 0 on error.
+ * Never blocks on the GPU. */
 long long CkFftCudaServerSubmit(CkFftCudaServer* server, const CkFftCudaJob* job);
 
 /* Waits for a ticket (timeout_s < 0: no limit).  1 when its results are
@@ -315,9 +320,15 @@ int CkFftCudaReplayPerRequest(CkFftContext* context, const CkFftCudaRequest* req
  * fixed 8 MiB device array compiled into the library, which every GPU that
  * loads the library holds until the process exits.  All calls on a device
  * share that array, so calls that overlap on the GPU race; order them (one
- * stream, or events).  The first call on a device looks up the array's
- * address; make that call before any stream capture.  stream == NULL blocks
- * until done; otherwise the work is enqueued on that cudaStream_t. */
+ * stream, or events).  The array's device address is looked up once per
+ * device when the first context is created on it (CkFftInit), so the 8 MiB is
+ * committed then and this call only reads the cached address; after a
+ * cudaDeviceReset, reload the library before using it again.  The first call
+ * of each size may still make the CUDA driver load that size's kernel code
+ * (lazy module loading; CUDA_MODULE_LOADING=EAGER loads everything up front),
+ * so make one call per size you use before the time-critical part and before
+ * any stream capture.  stream == NULL blocks until done; otherwise the work
+ * is enqueued on that cudaStream_t. */
 int CkFftCudaComplexBatchNoAlloc(CkFftContext* context, int n, int count, int inverse,
                                  const CkFftComplex* input, CkFftComplex* output, void* stream);
 

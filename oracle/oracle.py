@@ -25,7 +25,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF = os.path.join(HERE, "_ref")
-REF_TREE = "/root/reference"
+# the reference source tree (read only; present only where the reference was checked out)
+REF_TREE = os.environ.get("CKFFT_REFERENCE_TREE", "/root/reference")
 
 FORWARD, INVERSE, BOTH = 1, 2, 3
 KIND_CFWD, KIND_CINV, KIND_RFWD, KIND_RINV = 0, 1, 2, 3
@@ -37,7 +38,7 @@ def build(with_reference: bool | None = None) -> None:
     if with_reference is None:
         with_reference = os.path.isdir(os.path.join(REF_TREE, "src", "ckfft"))
     if with_reference:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
 
 
 def reference_available() -> bool:

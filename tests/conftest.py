@@ -70,6 +70,35 @@ def assert_close(got, ref, n, what=""):
     return e
 
 
+def assert_close_rows(got, ref, n, what="", chunk=2048):
+    """assert_close applied to every row of two 2-D arrays (one transform per
+    row), vectorised in chunks of rows; returns the worst relative L2 error."""
+    got = np.asarray(got)
+    ref = np.asarray(ref)
+    assert got.shape == ref.shape, (what, got.shape, ref.shape)
+    lim = ELEM_TOL_PER_LOG2 * max(1, int(np.log2(max(n, 1))))
+    dt = np.complex128 if np.iscomplexobj(ref) else np.float64
+    worst = 0.0
+    for s in range(0, got.shape[0], chunk):
+        r = ref[s:s + chunk].astype(dt)
+        d = np.abs(got[s:s + chunk].astype(dt) - r)
+        den = np.sqrt(np.sum(np.abs(r) ** 2, axis=1))
+        num = np.sqrt(np.sum(d ** 2, axis=1))
+        rel = np.where(den > 0, num / np.where(den > 0, den, 1.0), num)
+        i = int(np.argmax(rel))
+        assert rel[i] <= REL_L2_TOL, f"{what}: row {s + i} rel L2 {rel[i]:.3e} > {REL_L2_TOL}"
+        rms = den / np.sqrt(r.shape[1])
+        el = np.where(rms > 0, d.max(axis=1) / np.where(rms > 0, rms, 1.0), 0.0)
+        j = int(np.argmax(el))
+        assert el[j] <= lim, f"{what}: row {s + j} max element error {el[j]:.3e} rms > {lim:.3e}"
+        worst = max(worst, float(rel[i]))
+    return worst
+
+
+def host_threads():
+    return max(1, os.cpu_count() or 1)
+
+
 @pytest.fixture(scope="session")
 def torch_cuda():
     import torch

@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 from ckfft_gb300 import workloads  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 
-REF_TREE = "/root/reference"
+REF_TREE = os.environ.get("CKFFT_REFERENCE_TREE", "/root/reference")
 
 
 def read_input_txt():

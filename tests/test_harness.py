@@ -11,7 +11,7 @@ import pytest
 from conftest import ROOT
 
 HARNESS = os.path.join(ROOT, "ckfft_gb300", "_build", "ckfft_timing")
-TESTERS = ["ckfft", "ckfft_device", "kiss_fft", "ckfft_batch"]
+TESTERS = ["ckfft", "ckfft_device", "ckfft_kiss_api", "ckfft_batch"]
 
 
 def _gpu():

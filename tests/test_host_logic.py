@@ -66,3 +66,44 @@ def test_combine_ranks_takes_the_slowest_rank_gloo():
         t, v = out[r]
         assert t == 2.0
         assert v == pytest.approx(world * 1e9 / 2.0 / 1e9)
+
+
+def _shard_main(rank, world, port, frames, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+
+    sh = bench.frame_shard(rank, world, frames)
+    mine = torch.tensor([sh["start"], sh["count"], sh["seed"]], dtype=torch.int64)
+    every = [torch.zeros(3, dtype=torch.int64) for _ in range(world)]
+    dist.all_gather(every, mine)
+    out[rank] = [tuple(int(v) for v in t) for t in every]
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_frame_shards_are_disjoint_covering_and_seeded_per_rank_gloo():
+    """Each of two gloo ranks takes its shard of the weak-scaling run; the
+    gathered shards tile the job's frames exactly once, with one seed per rank."""
+    world, port, frames = 2, _free_port(), 65536
+    mgr = mp.get_context("spawn").Manager()
+    out = mgr.dict()
+    mp.start_processes(_shard_main, args=(world, port, frames, out), nprocs=world, start_method="spawn")
+    assert out[0] == out[1]
+    shards = sorted(out[0])
+    covered = np.zeros(world * frames, np.int32)
+    for start, count, _ in shards:
+        covered[start:start + count] += 1
+    assert np.all(covered == 1)
+    assert len({seed for _, _, seed in shards}) == world
+
+
+def test_bench_refuses_a_gpu_count_it_was_not_launched_with():
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--steps", "1"],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 2 and "WORLD_SIZE" in r.stderr, r.stderr

@@ -166,10 +166,14 @@ def test_plan_groups_multi_pass_sizes(torch_cuda, ctx_cache, oracle_mod):
     plan.close()
 
 
-def test_workload4_sample(torch_cuda, ctx_cache, oracle_mod):
-    """The uneven batch: 10000 transforms, log2 n in 6..16, 70% complex, 50% inverse."""
+def test_workload4_every_job(torch_cuda, ctx_cache, oracle_mod):
+    """The uneven batch: 10000 transforms, log2 n in 6..16, 70% complex, 50%
+    inverse, one graph replay; every job's output against the oracle (jobs of
+    one kind and size checked together through the oracle's threaded batch)."""
+    from conftest import assert_close_rows, host_threads
     from ckfft_gb300 import workloads as wl
     torch = torch_cuda
+    orc = oracle_mod
     spec = wl.uneven_jobs()
     rng = np.random.default_rng(wl.W4_SEED)
     ctx = ctx_cache(1 << 16)
@@ -179,10 +183,20 @@ def test_workload4_sample(torch_cuda, ctx_cache, oracle_mod):
         jobs.append(make_job(torch, rng, kind, 1 << l2, 1))
     plan = ctx.plan([as_tuple(j) for j in jobs])
     ctx.check(plan.exec(), "workload 4")
-    o = oracle_mod.Oracle(1 << 16)
-    for idx in list(range(0, 10000, 997)) + [9999]:
-        j = jobs[idx]
-        assert_close(j["out"].cpu().numpy()[0], oracle_out(o, j, 0), j["n"], f"job {idx}")
+    torch.cuda.synchronize()
+    o = orc.Oracle(1 << 16)
+    code = {"cfwd": orc.KIND_CFWD, "cinv": orc.KIND_CINV, "rfwd": orc.KIND_RFWD, "rinv": orc.KIND_RINV}
+    groups = {}
+    for idx, j in enumerate(jobs):
+        groups.setdefault((j["kind"], j["n"]), []).append(idx)
+    checked = 0
+    for (kind, n), idxs in sorted(groups.items()):
+        xs = np.stack([jobs[i]["x"][0] for i in idxs])
+        got = torch.stack([jobs[i]["out"][0] for i in idxs]).cpu().numpy()
+        ref = o.batch(code[kind], n, len(idxs), xs, host_threads())
+        assert_close_rows(got, ref, n, f"workload 4 {kind} n={n}")
+        checked += len(idxs)
+    assert checked == len(jobs) == wl.W4_JOBS
     plan.close()
 
 

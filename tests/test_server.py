@@ -121,8 +121,66 @@ def test_submit_validation(torch_cuda, ctx_cache, lib):
     b = torch.zeros(4096, dtype=torch.complex64, device="cuda")
     assert srv.submit("cfwd", 2048, 1, a, b) == 0          # n > nMax
     assert srv.submit("cfwd", 1024, 1, a, a) == 0          # in place
-    assert srv.submit("cfwd", 1024, 1, torch.zeros(1024, dtype=torch.complex64), b) == 0
+    assert srv.submit("cfwd", 1024, 1, None, b) == 0        # NULL input
     assert srv.wait(123456, 0.01)[0] == 0                  # unknown ticket
     t = srv.submit("cfwd", 1024, 2, a, b)
     assert t > 0 and srv.wait(t, 10.0)[0] == 1
+    srv.close()
+
+
+def test_workload5_shaped_mix_every_result(torch_cuda, ctx_cache, oracle_mod):
+    """Requests shaped like the serving workload -- 2^k points with k uniform
+    in 8..20, 1-64 frames, complex and real, forward and inverse, N(0,1)
+    inputs, every fourth request on page-locked host buffers (staged by the
+    server) -- submitted at once so that they share runs and direct lanes.
+    Every frame of every result is checked against the oracle, and each
+    request run alone gives the same bits as in the mix."""
+    from conftest import assert_close_rows, host_threads
+    from ckfft_gb300 import binding
+    from ckfft_gb300 import workloads as wl
+    torch = torch_cuda
+    orc = oracle_mod
+    nreq = 200
+    rng = np.random.default_rng(wl.W5_SEED)
+    lo, hi = wl.W5_LOG2
+    g = torch.Generator(device="cuda")
+    g.manual_seed(wl.W5_SEED)
+    reqs = []
+    for i in range(nreq):
+        kind = ["cfwd", "cinv", "rfwd", "rinv"][int(rng.integers(0, 4))]
+        n = 1 << int(rng.integers(lo, hi + 1))
+        count = int(rng.integers(1, 65))
+        if kind == "rfwd":
+            x = torch.randn((count, n), generator=g, device="cuda")
+            y = torch.full((count, n // 2 + 1), float("nan"), dtype=torch.complex64, device="cuda")
+        elif kind == "rinv":
+            x = torch.randn((count, n // 2 + 1), generator=g, device="cuda", dtype=torch.complex64)
+            y = torch.full((count, n), float("nan"), device="cuda")
+        else:
+            x = torch.randn((count, n), generator=g, device="cuda", dtype=torch.complex64)
+            y = torch.full((count, n), float("nan"), dtype=torch.complex64, device="cuda")
+        if i % 4 == 3:
+            x, y = x.cpu().pin_memory(), y.cpu().pin_memory()
+        reqs.append((kind, n, count, x, y))
+    ctx = ctx_cache(1 << hi)
+    srv = binding.Server(ctx, scratch_budget_bytes=2 << 30, max_inflight=3, direct_threshold_bytes=8 << 20)
+    tickets = [srv.submit(*r) for r in reqs]
+    assert all(t > 0 for t in tickets), binding.last_error()
+    for t in tickets:
+        ok, _ = srv.wait(t, 120.0)
+        assert ok, binding.last_error()
+    torch.cuda.synchronize()
+    code = {"cfwd": orc.KIND_CFWD, "cinv": orc.KIND_CINV, "rfwd": orc.KIND_RFWD, "rinv": orc.KIND_RINV}
+    o = orc.Oracle(1 << hi)
+    mixed = []
+    for i, (kind, n, count, x, y) in enumerate(reqs):
+        got = y.cpu().numpy()
+        ref = o.batch(code[kind], n, count, x.cpu().numpy(), host_threads())
+        assert_close_rows(got, ref, n, f"request {i}: {kind} n={n} x{count}")
+        mixed.append(bits(y))
+    for i, (r, m) in enumerate(zip(reqs, mixed)):      # alone: one request per run or lane
+        r[4].fill_(float("nan"))
+        ok, _ = srv.wait(srv.submit(*r), 120.0)
+        assert ok, binding.last_error()
+        assert bits(r[4]) == m, (i, r[0], r[1], r[2])
     srv.close()
