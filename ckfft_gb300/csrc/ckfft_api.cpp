@@ -143,7 +143,10 @@ Lane* acquire_lane(CkFftContext* c)
     Lane* l = new (std::nothrow) Lane();
     if (!l) return nullptr;
     for (int i = 0; i < kSlots; ++i) {
-        if (cudaStreamCreateWithFlags(&l->slot[i].stream, cudaStreamNonBlocking) != cudaSuccess) {
+        // blocking streams: a call made after work on the legacy default
+        // stream (a fill, a copy) sees that work done, as a synchronous
+        // library call should
+        if (cudaStreamCreateWithFlags(&l->slot[i].stream, cudaStreamDefault) != cudaSuccess) {
             for (int j = 0; j < i; ++j) cudaStreamDestroy(l->slot[j].stream);
             delete l;
             return nullptr;
@@ -345,7 +348,7 @@ size_t scratch_need(const Work& w, long long cnt)
 {
     if (!needs_large(w)) return 0;
     if (!is_real(w.kind) && ckg::cluster_supported(w.log2n) && ckg::cluster_enabled()) return 0;
-    if (!is_real(w.kind) && ckg::mid_supported(w.log2n) && ckg::mid_enabled())
+    if (!is_real(w.kind) && ckg::mid_supported(w.log2n) && ckg::mid_enabled(w.log2n))
         return ckg::mid_scratch_bytes(w.log2n, cnt);
     const size_t one = ckg::large_scratch_bytes(w.kind, w.log2n);
     const size_t cap = 256ull << 20;

@@ -37,15 +37,21 @@ bool cluster_enabled()
     return on;
 }
 
-// Off unless CKFFT_CUDA_MID=1 (otherwise the cluster two-pass kernel of
-// fft_l2pass.cu runs complex 2^15 / 2^16).
-bool mid_enabled()
+// Opt-in (CKFFT_CUDA_MID=1): the persistent kernel of fft_mid.cu for complex
+// 2^15 / 2^16.  Measured on GB300 (batches of 1 GiB, GB/s) against the
+// cluster two-pass kernel of fft_l2pass.cu that runs these sizes by default:
+// 2^15 3201 vs 3313, 2^16 3189 vs 3491 (earlier builds of it measured up to
+// 3529 / 3429); both are bound by the two passes' instructions, and the
+// persistent form, holding a whole SM per CTA, also keeps other kernels of a
+// mixed run off its SMs (the uneven batch fell from 3217 to 2983 GB/s with
+// its grouped 2^15 launches on it).
+bool mid_enabled(int log2n)
 {
     static const bool on = [] {
         const char* v = std::getenv("CKFFT_CUDA_MID");
         return v && v[0] == '1';
     }();
-    return on;
+    return on && mid_supported(log2n);
 }
 
 static std::atomic<long long> g_launches{0};

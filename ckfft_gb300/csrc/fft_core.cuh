@@ -277,6 +277,53 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[1 << LOG2R], int t, co
     });
 }
 
+// The same stage with its table twiddles loaded beforehand: wb[u][i] holds
+// W^(2^i k_u) for butterfly u (stage_twiddles); the other powers are products
+// as in stage_compute.  For kernels that run the same stage on many tiles,
+// where k_u does not change from tile to tile.
+template <int LOG2N, int LOG2R, int LRS, int LNS, bool INV>
+__device__ __forceinline__ void stage_twiddles(int t, const float2* __restrict__ tw,
+                                               float2 (&wb)[(1 << LOG2R) >> LRS][LRS])
+{
+    constexpr int R = 1 << LOG2R, RS = 1 << LRS, NS = 1 << LNS;
+    constexpr int T = (1 << LOG2N) / R;
+    constexpr int U = R / RS;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int k = (t + u * T) & (NS - 1);
+#pragma unroll
+        for (int i = 0; i < LRS; ++i) wb[u][i] = tw_load<INV>(tw + NS * RS / (1 << i), k);
+    }
+}
+
+template <int LOG2N, int LOG2R, int LRS, int LNS, bool INV>
+__device__ __forceinline__ void stage_compute_pre(float2 (&v)[1 << LOG2R], const float2 (&wb)[(1 << LOG2R) >> LRS][LRS])
+{
+    constexpr int R = 1 << LOG2R, RS = 1 << LRS;
+    constexpr int U = R / RS;
+    static_assert((1 << LNS) > 1, "the first stage has no twiddles");
+    static_for<0, U>([&](auto uc) {
+        constexpr int u = decltype(uc)::value;
+        float2 x[RS];
+#pragma unroll
+        for (int j = 0; j < RS; ++j) x[j] = v[u + j * U];
+        float2 w[RS];
+#pragma unroll
+        for (int i = 0; i < LRS; ++i) w[1 << i] = wb[u][i];
+#pragma unroll
+        for (int j = 3; j < RS; ++j) {
+            if ((j & (j - 1)) == 0) continue;
+            const int hb = 1 << (31 - __clz(j));
+            w[j] = cmul(w[hb], w[j - hb]);
+        }
+#pragma unroll
+        for (int j = 1; j < RS; ++j) x[j] = cmul(x[j], w[j]);
+        dft<RS, INV>(x);
+#pragma unroll
+        for (int j = 0; j < RS; ++j) v[u + j * U] = x[j];
+    });
+}
+
 // Writes a stage's outputs to their Stockham positions, then reloads the
 // thread's registers with positions t + m*T.
 template <int LOG2N, int LOG2R, int LRS, int LNS, bool WARP, int BAR_ID = 0, int BAR_N = 0, class View>

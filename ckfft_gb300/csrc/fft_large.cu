@@ -377,7 +377,7 @@ cudaError_t launch_large_c2c(bool inverse, int log2n, const void* in, void* out,
     // 2^15, 2^16: both passes inside one persistent CTA per transform
     // (fft_mid.cu), or inside one cluster per transform (fft_l2pass.cu); the
     // intermediate kept in L2 either way
-    if (mid_supported(log2n) && mid_enabled() && ((uintptr_t)scratch & 127) == 0 && ((uintptr_t)in & 15) == 0 &&
+    if (mid_supported(log2n) && mid_enabled(log2n) && ((uintptr_t)scratch & 127) == 0 && ((uintptr_t)in & 15) == 0 &&
         (in_dist & 1) == 0 && scratch_bytes >= mid_scratch_bytes(log2n, count))
         return launch_mid(inverse ? 1 : 0, log2n, in, out, count, in_dist, out_dist, tw, scratch, scratch_bytes, s);
     if (l2pass_supported(log2n) && ((uintptr_t)scratch & 127) == 0)

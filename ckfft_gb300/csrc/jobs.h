@@ -65,8 +65,6 @@ cudaError_t launch_group(int op, int log2a, const FrameDesc* fr, long long count
                          void* scratch, size_t scratch_bytes, cudaStream_t s);
 cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
                                 void* scratch, size_t scratch_bytes, cudaStream_t s);
-cudaError_t launch_mid_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
-                             void* scratch, size_t scratch_bytes, cudaStream_t s);
 cudaError_t launch_r2c_table(int lm, const FrameDesc* fr, long long count, const float2* tw, void* scratch,
                              size_t scratch_bytes, cudaStream_t s);
 cudaError_t launch_c2r_table(int lm, const FrameDesc* fr, long long count, const float2* tw, void* scratch,
@@ -130,10 +128,11 @@ struct RunSlot {
 void free_run_slot(RunSlot* r);
 // Validates, builds and enqueues a mixed run on `s` with the slot's buffers.
 // 1 on success, 0 on invalid jobs, -1 on a CUDA failure (message set).
-// scratch_override: caller-owned intermediates (>= the run's scratch bytes);
-// NULL uses (and grows) the slot's own scratch.
+// scratch_override: caller-owned intermediates of scratch_override_bytes
+// (a run needing more fails with -1); NULL uses (and grows) the slot's own
+// scratch.
 int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunSlot* r, cudaStream_t s,
-                float2* scratch_override = nullptr);
+                float2* scratch_override = nullptr, size_t scratch_override_bytes = 0);
 bool validate_job(const ContextView& cv, const CkFftCudaJob& j, int index, bool allow_host = false);
 long long job_scratch_bytes(const CkFftCudaJob& j);
 long long job_algo_bytes(const CkFftCudaJob& j);

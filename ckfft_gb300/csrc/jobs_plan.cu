@@ -437,11 +437,15 @@ static cudaError_t grow_dev(void** p, size_t* cap, size_t need)
 }
 
 int enqueue_run(const ContextView& cv, const CkFftCudaJob* jobs, int njobs, RunSlot* r, cudaStream_t s,
-                float2* scratch_override)
+                float2* scratch_override, size_t scratch_override_bytes)
 {
     Built b;
     if (!build_units(cv, jobs, njobs, &b)) return 0;
     if (b.empty()) return 1;
+    if (scratch_override && sizeof(float2) * (size_t)b.scratch_elems > scratch_override_bytes) {
+        set_last_error("the run's intermediates exceed the scratch it was given");
+        return -1;
+    }
     const RunLayout lay = run_layout(b);
     const size_t o_recs = lay.recs, o_done = lay.done, total = lay.total;
     cudaError_t e = cudaSuccess;

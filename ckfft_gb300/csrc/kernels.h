@@ -118,9 +118,10 @@ cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long l
 // both passes inside the CTA with bulk-copied tiles and the intermediate in
 // L2 (fft_mid.cu).  scratch: mid_scratch_bytes(), 128-byte aligned; in
 // 16-byte aligned, in_dist even.  kind 0 / 1: forward / inverse.
-// mid_enabled(): only with CKFFT_CUDA_MID=1.
+// mid_enabled(log2n): only with CKFFT_CUDA_MID=1 (opt-in; the cluster
+// two-pass kernel of fft_l2pass.cu measured as fast or faster).
 bool mid_supported(int log2n);
-bool mid_enabled();
+bool mid_enabled(int log2n);
 size_t mid_scratch_bytes(int log2n, long long count);
 cudaError_t launch_mid(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,
                        long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes, cudaStream_t stream);

@@ -334,15 +334,20 @@ void dispatch_loop(CkFftCudaServer* s)
             }
             sl.reqs = std::move(batch);
             float2* override_scratch = nullptr;
+            size_t override_bytes = 0;
             bool ok = true;
             if (oversized) {
                 ok = ckg::pool_alloc_async((void**)&sl.pooled, (size_t)scratch, sl.stream) == cudaSuccess;
                 override_scratch = sl.pooled;
+                override_bytes = (size_t)scratch;
             } else if (scratch) {
                 override_scratch = sl.run.scratch;
+                override_bytes = sl.run.scratch_cap;
             }
             ok = ok && stage_inputs(sl.reqs, jobs, &sl.stage, sl.stream) == cudaSuccess;
-            const int rc = ok ? ckg::enqueue_run(s->cv, jobs.data(), (int)jobs.size(), &sl.run, sl.stream, override_scratch) : -1;
+            const int rc = ok ? ckg::enqueue_run(s->cv, jobs.data(), (int)jobs.size(), &sl.run, sl.stream, override_scratch,
+                                                 override_bytes)
+                              : -1;
             if (rc == 1 && stage_outputs(sl.reqs, jobs, sl.stream) == cudaSuccess &&
                 cudaEventRecord(sl.ev, sl.stream) == cudaSuccess) {
                 sl.busy = true;
