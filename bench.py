@@ -78,6 +78,30 @@ def parse_args():
     return ap.parse_args()
 
 
+VARIANT_SHAPE = {0: "", 2: "pipelined, 2 bulk-copy buffers", 3: "pipelined, 3 bulk-copy buffers",
+                 4: "half the values per thread", 5: "twice the values per thread",
+                 6: "CTAs of about 512 threads", 7: "CTAs of about 128 threads"}
+
+
+def kernel_label(kind, n):
+    """The single-CTA kernel (and tuned variant) the library runs for a batch
+    of this kind and size, from the committed tuning table."""
+    kinds = ["cfwd", "cinv", "rfwd", "rinv"]
+    lc = int(math.log2(n)) - (1 if kind[0] == "r" else 0)
+    v = 0
+    path = os.path.join(ROOT, "ckfft_gb300", "csrc", "tuning_table.h")
+    if os.path.exists(path):
+        rows = re.findall(r"\{([0-9, ]+)\},\s*//\s*(\w+)", open(path).read())
+        table = {name: [int(x) for x in row.split(",")] for row, name in rows}
+        if kind in table and lc < len(table[kind]):
+            v = table[kind][lc]
+    name = {"cfwd": "k_c2c_small", "cinv": "k_c2c_small", "rfwd": "k_r2c_small", "rinv": "k_c2r_small"}[kind]
+    if v in (2, 3):
+        name = "k_pipe"
+    shape = VARIANT_SHAPE.get(v, "")
+    return f"{name}<{lc}>" + (f" ({shape})" if shape else "")
+
+
 def frame_bytes(n):
     from ckfft_gb300.workloads import algorithmic_bytes
 
@@ -347,7 +371,7 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": f"real FFT N={n} FP32, {frames} frames per GPU, forward + inverse batch",
                    "n": n, "frames": frames, "parallelism": f"replicas x{world} (frames sharded, no collective)",
                    "l2": "inputs larger than L2 (1 GiB of frames per direction), no flush needed"},
-        "roofline": {"bound": "hbm", "kernel": "k_r2c_small<11> (real forward, n=4096)",
+        "roofline": {"bound": "hbm", "kernel": kernel_label("rfwd", n) + f", real forward n={n}",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "traffic": traffic, "algorithmic_bytes_per_launch": frames * frame_bytes(n),
@@ -525,7 +549,7 @@ def run_w1(args):
     line = base_line(args, "batched complex FFT GB/s (N=1024 FP32, fwd+inv)", value, "GB/s", secs,
                      {"workload": f"complex FFT n={n}, {frames} frames, forward then inverse (round trip)",
                       "n": n, "frames": frames, "l2": "256 MiB buffer written between timed steps (outside the events)"})
-    line["roofline"] = {"bound": "hbm", "kernel": "k_c2c_small<10> (complex forward, n=1024)",
+    line["roofline"] = {"bound": "hbm", "kernel": kernel_label("cfwd", n) + f", complex forward n={n}",
                         "achieved": round(frames * per / (fwd_ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
                         "frac": round(frames * per / (fwd_ms / 1e3) / 1e9 / peak, 4), "peak_source": src,
                         "traffic": None, "avg_launch_ms": round(fwd_ms, 4)}

@@ -21,6 +21,19 @@ cudaError_t prepare_fused();
 cudaError_t prepare_inter();
 cudaError_t prepare_l2pass();
 cudaError_t prepare_groups();
+cudaError_t prepare_shape_halfr();
+cudaError_t prepare_shape_doubler();
+cudaError_t prepare_shape_cta512();
+cudaError_t prepare_shape_cta128();
+#define CKG_SHAPE_DECL(name)                                                                                     \
+    cudaError_t launch_shape_##name(Kind kind, int log2c, const void* in, void* out, long long count,          \
+                                    long long in_dist, long long out_dist, const float2* tw, cudaStream_t s,   \
+                                    bool* done);
+CKG_SHAPE_DECL(halfr)
+CKG_SHAPE_DECL(doubler)
+CKG_SHAPE_DECL(cta512)
+CKG_SHAPE_DECL(cta128)
+#undef CKG_SHAPE_DECL
 cudaError_t prepare_noalloc();
 cudaError_t prepare_mid();
 
@@ -74,6 +87,18 @@ cudaError_t launch_small(Kind kind, int log2n, const void* in, void* out, long l
     return e;
 }
 
+cudaError_t launch_small_shape(Kind kind, int v, int log2c, const void* in, void* out, long long count,
+                               long long in_dist, long long out_dist, const float2* tw, cudaStream_t s, bool* done)
+{
+    switch (v) {
+    case 4: return launch_shape_halfr(kind, log2c, in, out, count, in_dist, out_dist, tw, s, done);
+    case 5: return launch_shape_doubler(kind, log2c, in, out, count, in_dist, out_dist, tw, s, done);
+    case 6: return launch_shape_cta512(kind, log2c, in, out, count, in_dist, out_dist, tw, s, done);
+    case 7: return launch_shape_cta128(kind, log2c, in, out, count, in_dist, out_dist, tw, s, done);
+    default: *done = false; return cudaSuccess;
+    }
+}
+
 static thread_local int t_plain_loads = 0;
 
 PlainLoadsScope::PlainLoadsScope() : prev(t_plain_loads) { t_plain_loads = 1; }
@@ -83,10 +108,10 @@ int variant_for(Kind kind, int log2c)
 {
     if (t_plain_loads) return 0;
     static const int forced = [] {
-        const char* v = std::getenv("CKFFT_CUDA_PIPE_NBUF");
+        const char* v = std::getenv("CKFFT_CUDA_VARIANT");
         if (!v || !*v) return -1;
         const int x = std::atoi(v);
-        return (x == 0 || x == 2 || x == 3) ? x : -1;
+        return (x == 0 || (x >= 2 && x <= 7)) ? x : -1;
     }();
     if (forced >= 0) return forced;
     if (kind < 0 || kind > 3 || log2c < 0 || log2c > 14) return 0;
@@ -215,6 +240,10 @@ cudaError_t prepare_device()
     if ((e = prepare_inter()) != cudaSuccess) return e;
     if ((e = prepare_l2pass()) != cudaSuccess) return e;
     if ((e = prepare_groups()) != cudaSuccess) return e;
+    if ((e = prepare_shape_halfr()) != cudaSuccess) return e;
+    if ((e = prepare_shape_doubler()) != cudaSuccess) return e;
+    if ((e = prepare_shape_cta512()) != cudaSuccess) return e;
+    if ((e = prepare_shape_cta128()) != cudaSuccess) return e;
     if ((e = prepare_noalloc()) != cudaSuccess) return e;
     if ((e = prepare_mid()) != cudaSuccess) return e;
     if (dev < 64) done |= 1ull << dev;

@@ -25,11 +25,11 @@ struct InterCfg {
     // threads and the shared memory allow, else 4 (2 at 2^13)
     static constexpr int G = S::TPB >= 16 ? S::TPB : L <= 10 ? 16 : L == 11 ? 8 : L == 12 ? 4 : 2;
     static constexpr int THREADS = T * G;
-    static constexpr int MINB = 1024 / THREADS > 0 ? 1024 / THREADS : 1;
+    // resident CTAs asked of ptxas: 64 registers a thread up to 16 values, 128 for 32
+    static constexpr int MINB = (R <= 16 ? 1024 : 512) / THREADS > 0 ? (R <= 16 ? 1024 : 512) / THREADS : 1;
     static constexpr bool WARP = S::WARP;
     static constexpr int SLOT = S::SLOT;
     static constexpr size_t SMEM = sizeof(float2) * (size_t)SLOT * G;
-    static_assert(R == 16, "the interleaved shapes hold 16 values per thread");
     static_assert(THREADS <= 1024, "one CTA");
 };
 

@@ -9,16 +9,30 @@
 #pragma once
 #include "fft_core.cuh"
 #include "kernels.h"
+#include "tuning_table.h"
 
 namespace ckg {
 
-// Per-size launch shape: R values per thread, TPB transforms per CTA.
-template <int L>
+// Values per thread (log2) for a transform of 2^L points: the autotuned
+// choice (tuning_table.h), the same for every kernel family of the size so
+// that batched, pipelined, strided, fused and grouped kernels compute it
+// with the same radices and produce the same bits.
+__host__ __device__ constexpr int default_log2r(int L)
+{
+    return (L >= 0 && L < (int)(sizeof(kTunedLog2R) / sizeof(kTunedLog2R[0]))) ? kTunedLog2R[L] : 5;
+}
+
+// Per-size launch shape: R = 2^LR values per thread, T = n/R threads per
+// transform, TPB transforms per CTA filling about CTH threads.  The default
+// shape is the one most callers use; the batched kernels also come in the
+// other shapes the autotuner measures (half / double the values per thread,
+// 512- or 128-thread CTAs).
+template <int L, int LR = default_log2r(L), int CTH = 256>
 struct SmallCfg {
-    static constexpr int LOG2R = L < 4 ? L : L < 14 ? 4 : 5;
+    static constexpr int LOG2R = LR;
     static constexpr int R = 1 << LOG2R;
     static constexpr int T = (1 << L) / R;
-    static constexpr int TPB = T >= 256 ? 1 : 256 / T;
+    static constexpr int TPB = T >= CTH ? 1 : CTH / T;
     static constexpr int THREADS = T * TPB;
     // resident CTAs asked of ptxas: 64 registers per thread for R <= 16, 128 for R = 32
     static constexpr int MINB = (R <= 16 ? 1024 : 512) / THREADS > 0 ? (R <= 16 ? 1024 : 512) / THREADS : 1;
@@ -125,11 +139,10 @@ __device__ __forceinline__ void split_store(const View& view, const Dst& dst, in
 // touching memory.  Used by the batched kernels below and by the persistent
 // job kernel (fft_jobs.cu).
 
-template <int L, bool INV, class Src, class Dst>
+template <int L, bool INV, class Src, class Dst, class C = SmallCfg<L>>
 __device__ __forceinline__ void frame_c2c_at(const Src& src, const Dst& dst, bool live, int t,
                                              const PaddedView& view, const float2* __restrict__ tw)
 {
-    using C = SmallCfg<L>;
     float2 v[C::R];
     if (live) {
 #pragma unroll
@@ -153,11 +166,10 @@ __device__ __forceinline__ void frame_c2c(const float2* __restrict__ src, float2
 }
 
 // Real forward: n = 2M reals (read as M packed pairs) -> M+1 complex bins (2 DFT).
-template <int LM, class Src, class Dst>
+template <int LM, class Src, class Dst, class C = SmallCfg<LM>>
 __device__ __forceinline__ void frame_r2c_at(const Src& src, const Dst& dst, bool live, int t,
                                              const PaddedView& view, const float2* __restrict__ tw)
 {
-    using C = SmallCfg<LM>;
     constexpr int M = 1 << LM;
     float2 v[C::R];
     if (live) {
@@ -184,11 +196,10 @@ __device__ __forceinline__ void frame_r2c(const float2* __restrict__ src, float2
 
 // Real inverse: M+1 complex bins -> n = 2M reals (written as M packed pairs).
 // The real inverse's first step: v[m] = merge(X[p], X[M-p]) at p = t + mT.
-template <int LM, class Src>
+template <int LM, class Src, class C = SmallCfg<LM>>
 __device__ __forceinline__ void c2r_load(const Src& src, bool live, int t, const float2* __restrict__ tw,
-                                         float2 (&v)[SmallCfg<LM>::R])
+                                         float2 (&v)[C::R])
 {
-    using C = SmallCfg<LM>;
     constexpr int M = 1 << LM;
     const float2* twn = tw + 2 * M;
     if (live) {
@@ -211,13 +222,12 @@ __device__ __forceinline__ void c2r_load(const Src& src, bool live, int t, const
     }
 }
 
-template <int LM, class Src, class Dst>
+template <int LM, class Src, class Dst, class C = SmallCfg<LM>>
 __device__ __forceinline__ void frame_c2r_at(const Src& src, const Dst& dst, bool live, int t,
                                              const PaddedView& view, const float2* __restrict__ tw)
 {
-    using C = SmallCfg<LM>;
     float2 v[C::R];
-    c2r_load<LM>(src, live, t, tw, v);
+    c2r_load<LM, Src, C>(src, live, t, tw, v);
     stockham<LM, C::LOG2R, true, C::WARP>(v, t, tw, view);
     if (live) {
 #pragma unroll
@@ -335,12 +345,12 @@ __device__ __forceinline__ void block_c2r(const float2* __restrict__ in, float2*
         __stcs(dst + i, smem[(i >> LM) * C::SLOT + PaddedView::pad(i & (M - 1))]);
 }
 
-template <int L, bool INV>
-__global__ void __launch_bounds__(SmallCfg<L>::THREADS, SmallCfg<L>::MINB)
+template <int L, bool INV, int LR = default_log2r(L), int CTH = 256>
+__global__ void __launch_bounds__(SmallCfg<L, LR, CTH>::THREADS, SmallCfg<L, LR, CTH>::MINB)
 k_c2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
-    using C = SmallCfg<L>;
+    using C = SmallCfg<L, LR, CTH>;
     pdl_start();
     extern __shared__ float2 smem[];
     if constexpr (C::T <= 2 && L >= 2) {
@@ -351,15 +361,16 @@ k_c2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
     }
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
     const long long f = (long long)blockIdx.x * C::TPB + g;
-    frame_c2c<L, INV>(in + f * in_dist, out + f * out_dist, f < count, t, PaddedView{smem + g * C::SLOT}, tw);
+    frame_c2c_at<L, INV, RowIn, RowOut, C>(RowIn{in + f * in_dist}, RowOut{out + f * out_dist}, f < count, t,
+                                           PaddedView{smem + g * C::SLOT}, tw);
 }
 
-template <int LM>
-__global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
+template <int LM, int LR = default_log2r(LM), int CTH = 256>
+__global__ void __launch_bounds__(SmallCfg<LM, LR, CTH>::THREADS, SmallCfg<LM, LR, CTH>::MINB)
 k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
-    using C = SmallCfg<LM>;
+    using C = SmallCfg<LM, LR, CTH>;
     pdl_start();
     extern __shared__ float2 smem[];
     if constexpr (C::T <= 2) {
@@ -370,15 +381,16 @@ k_r2c_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
     }
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
     const long long f = (long long)blockIdx.x * C::TPB + g;
-    frame_r2c<LM>(in + f * in_dist, out + f * out_dist, f < count, t, PaddedView{smem + g * C::SLOT}, tw);
+    frame_r2c_at<LM, RowIn, RowOut, C>(RowIn{in + f * in_dist}, RowOut{out + f * out_dist}, f < count, t,
+                                       PaddedView{smem + g * C::SLOT}, tw);
 }
 
-template <int LM>
-__global__ void __launch_bounds__(SmallCfg<LM>::THREADS, SmallCfg<LM>::MINB)
+template <int LM, int LR = default_log2r(LM), int CTH = 256>
+__global__ void __launch_bounds__(SmallCfg<LM, LR, CTH>::THREADS, SmallCfg<LM, LR, CTH>::MINB)
 k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long count,
             long long in_dist, long long out_dist, const float2* __restrict__ tw)
 {
-    using C = SmallCfg<LM>;
+    using C = SmallCfg<LM, LR, CTH>;
     pdl_start();
     extern __shared__ float2 smem[];
     if constexpr (C::T <= 2) {
@@ -389,7 +401,8 @@ k_c2r_small(const float2* __restrict__ in, float2* __restrict__ out, long long c
     }
     const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
     const long long f = (long long)blockIdx.x * C::TPB + g;
-    frame_c2r<LM>(in + f * in_dist, out + f * out_dist, f < count, t, PaddedView{smem + g * C::SLOT}, tw);
+    frame_c2r_at<LM, RowIn, RowOut, C>(RowIn{in + f * in_dist}, RowOut{out + f * out_dist}, f < count, t,
+                                       PaddedView{smem + g * C::SLOT}, tw);
 }
 
 // ---------------------------------------------------------------- launch
@@ -400,47 +413,68 @@ inline unsigned small_grid(long long count)
     return (unsigned)((count + C::TPB - 1) / C::TPB);
 }
 
-template <int L, bool INV>
+template <int L, bool INV, int LR = default_log2r(L), int CTH = 256>
 cudaError_t launch_c2c_L(const void* in, void* out, long long count, long long in_dist,
                          long long out_dist, const float2* tw, cudaStream_t s)
 {
-    using C = SmallCfg<L>;
-    return launch_pdl(k_c2c_small<L, INV>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
+    using C = SmallCfg<L, LR, CTH>;
+    return launch_pdl(k_c2c_small<L, INV, LR, CTH>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
                       (const float2*)in, (float2*)out, count, in_dist, out_dist, tw);
 }
 
-template <int LM>
+template <int LM, int LR = default_log2r(LM), int CTH = 256>
 cudaError_t launch_r2c_L(const void* in, void* out, long long count, long long in_dist,
                          long long out_dist, const float2* tw, cudaStream_t s)
 {
-    using C = SmallCfg<LM>;
-    return launch_pdl(k_r2c_small<LM>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
+    using C = SmallCfg<LM, LR, CTH>;
+    return launch_pdl(k_r2c_small<LM, LR, CTH>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
                       (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw);
 }
 
-template <int LM>
+template <int LM, int LR = default_log2r(LM), int CTH = 256>
 cudaError_t launch_c2r_L(const void* in, void* out, long long count, long long in_dist,
                          long long out_dist, const float2* tw, cudaStream_t s)
 {
-    using C = SmallCfg<LM>;
-    return launch_pdl(k_c2r_small<LM>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
+    using C = SmallCfg<LM, LR, CTH>;
+    return launch_pdl(k_c2r_small<LM, LR, CTH>, dim3(small_grid<C>(count)), dim3(C::THREADS), C::SMEM, s,
                       (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw);
 }
 
-template <int L, bool INV>
+template <int L, bool INV, int LR = default_log2r(L), int CTH = 256>
 cudaError_t attr_c2c_L()
 {
-    return cudaFuncSetAttribute(k_c2c_small<L, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)SmallCfg<L>::SMEM);
+    return cudaFuncSetAttribute(k_c2c_small<L, INV, LR, CTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SmallCfg<L, LR, CTH>::SMEM);
 }
-template <int LM>
+template <int LM, int LR = default_log2r(LM), int CTH = 256>
 cudaError_t attr_real_L()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_r2c_small<LM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SmallCfg<LM>::SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_r2c_small<LM, LR, CTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SmallCfg<LM, LR, CTH>::SMEM);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_c2r_small<LM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)SmallCfg<LM>::SMEM);
+    return cudaFuncSetAttribute(k_c2r_small<LM, LR, CTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SmallCfg<LM, LR, CTH>::SMEM);
 }
+
+// ---------------------------------------------------------- tuned shapes
+// Kernel variants of a single-CTA size (variant_for): 0 the default shape,
+// 2 / 3 the pipelined kernel (fft_pipe.cuh), 4 half the values per thread,
+// 5 twice the values per thread, 6 CTAs of about 512 threads, 7 of about 128.
+constexpr int kVariantHalfR = 4, kVariantDoubleR = 5, kVariantCta512 = 6, kVariantCta128 = 7;
+
+template <int L, int V>
+struct ShapeOf {
+    static constexpr int LR0 = default_log2r(L);
+    static constexpr int LR = V == kVariantHalfR ? LR0 - 1 : V == kVariantDoubleR ? LR0 + 1 : LR0;
+    static constexpr int CTH = V == kVariantCta512 ? 512 : V == kVariantCta128 ? 128 : 256;
+    static constexpr int T0 = 1 << (L - LR0);
+    // a shape exists when it differs from the default and fits: 2..32 values
+    // per thread, at most 1024 threads per transform, room in shared memory
+    static constexpr bool kValid =
+        L >= 6 && LR >= 1 && LR <= 5 && LR <= L && (L - LR) <= 10 &&
+        (V == kVariantHalfR || V == kVariantDoubleR || (V == kVariantCta512 && T0 < 512) ||
+         (V == kVariantCta128 && T0 < 256)) &&
+        SmallCfg<L, (LR >= 1 ? LR : 1), CTH>::SMEM <= 227 * 1024;
+};
 
 }  // namespace ckg

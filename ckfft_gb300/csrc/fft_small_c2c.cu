@@ -1,6 +1,6 @@
 // fft_small_c2c.cu -- instantiates the single-CTA complex kernels (2^0 .. 2^14):
 // the pipelined persistent kernel for whole frame groups, the plain kernel for
-// the rest.
+// the rest; the tuned shape variants live in fft_shape_*.cu.
 #include "fft_pipe.cuh"
 
 namespace ckg {
@@ -14,6 +14,12 @@ static cudaError_t launch_c2c_any(const void* in, void* out, long long count, lo
     if constexpr (L >= kPipeMinLog2) {
         constexpr int K = INV ? C2C_INV : C2C_FWD;
         const int nb = variant_for((Kind)K, L);
+        if (nb >= 4) {
+            bool shaped = false;
+            e = launch_small_shape((Kind)K, nb, L, in, out, count, in_dist, out_dist, tw, s, &shaped);
+            if (shaped && e == cudaSuccess) count_launch();
+            if (shaped || e != cudaSuccess) return e;
+        }
         if (nb == 2) e = launch_pipe<L, K, 2>(in, out, count, in_dist, out_dist, tw, device_error_word(), s, &done);
         else if (nb == 3) e = launch_pipe<L, K, 3>(in, out, count, in_dist, out_dist, tw, device_error_word(), s, &done);
         if (e != cudaSuccess) return e;

@@ -15,6 +15,12 @@ static cudaError_t launch_real_any(const void* in, void* out, long long count, l
         constexpr int K = INV ? C2R : R2C;
         const long long di = INV ? in_dist : in_dist / 2, dout = INV ? out_dist / 2 : out_dist;
         const int nb = variant_for((Kind)K, LM);
+        if (nb >= 4) {
+            bool shaped = false;
+            e = launch_small_shape((Kind)K, nb, LM, in, out, count, in_dist, out_dist, tw, s, &shaped);
+            if (shaped && e == cudaSuccess) count_launch();
+            if (shaped || e != cudaSuccess) return e;
+        }
         if (nb == 2) e = launch_pipe<LM, K, 2>(in, out, count, di, dout, tw, device_error_word(), s, &done);
         else if (nb == 3) e = launch_pipe<LM, K, 3>(in, out, count, di, dout, tw, device_error_word(), s, &done);
         if (e != cudaSuccess) return e;

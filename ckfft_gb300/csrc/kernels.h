@@ -171,11 +171,19 @@ void set_last_error(const char* msg);
 
 // Smallest log2 (complex) length served by the pipelined persistent kernels.
 constexpr int kPipeMinLog2 = 6;
-// Kernel variant for a single-CTA size: 0 plain, 2 / 3 pipelined with that
-// many bulk-copy buffers.  From the committed autotune table (tuning_table.h)
-// unless the CKFFT_CUDA_PIPE_NBUF environment variable forces one variant
-// (the autotuner uses it to measure each variant).
+// Kernel variant for a single-CTA size: 0 plain (default shape), 2 / 3
+// pipelined with that many bulk-copy buffers, 4 / 5 half / twice the values
+// per thread, 6 / 7 CTAs of about 512 / 128 threads.  From the committed
+// autotune table (tuning_table.h) unless the CKFFT_CUDA_VARIANT environment
+// variable forces one variant (the autotuner uses it to measure each);
+// a variant that does not exist for a size runs the plain kernel.
 int variant_for(Kind kind, int log2c);
+// The batched single-CTA kernels in shape variant v (4..7) for complex
+// (half-)length 2^log2c, dists as the plain launchers take them; *done is
+// false when that variant does not exist for the size (nothing launched).
+cudaError_t launch_small_shape(Kind kind, int v, int log2c, const void* in, void* out, long long count,
+                               long long in_dist, long long out_dist, const float2* tw, cudaStream_t stream,
+                               bool* done);
 // While one of these lives on a thread, variant_for() answers 0 on that
 // thread: launches whose input is host memory mapped into the device's
 // address space read it with plain loads, never with bulk (TMA) copies.
