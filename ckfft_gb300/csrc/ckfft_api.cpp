@@ -94,6 +94,8 @@ struct Lane {
     Slot slot[kSlots];
     void* scratch = nullptr;
     size_t scratch_cap = 0;
+    void* bounce = nullptr;     // page-locked, mapped: small calls on pageable host memory
+    size_t bounce_cap = 0;
     bool busy = false;
 };
 
@@ -172,6 +174,7 @@ void free_lane(Lane* l)
         if (l->slot[i].stream) cudaStreamDestroy(l->slot[i].stream);
     }
     cudaFree(l->scratch);
+    if (l->bounce) cudaFreeHost(l->bounce);
     delete l;
 }
 
@@ -405,6 +408,63 @@ int run_direct(CkFftContext* c, const Work& w, const void* in, void* out, bool h
     return 1;
 }
 
+// Calls on pageable host memory up to this many bytes per side bounce
+// through the lane's page-locked buffer: the CPU copies the input in, the
+// kernel reads and writes the page-locked memory in place over the CPU-GPU
+// link, the CPU copies the output out.  Two cudaMemcpy of pageable memory
+// cost about 14 us on GB300 for 8 KiB each way (they are synchronous and
+// staged by the driver); the two host copies take well under 1 us.
+constexpr size_t kBounceMaxBytes = 1u << 20;
+
+bool bounce_pays(const Work& w, Mem min, Mem mout)
+{
+    if (needs_large(w) || (min != Mem::Host && mout != Mem::Host)) return false;
+    return (size_t)w.count * w.in_bytes <= kBounceMaxBytes && (size_t)w.count * w.out_bytes <= kBounceMaxBytes;
+}
+
+int run_bounce(CkFftContext* c, const Work& w, const void* in, void* out, Mem min, Mem mout)
+{
+    Lane* lane = acquire_lane(c);
+    if (!lane) return fail("cannot create a staging lane (CUDA streams)");
+    const size_t ib = (size_t)w.count * w.in_bytes, ob = (size_t)w.count * w.out_bytes;
+    const size_t ibr = (ib + 255) / 256 * 256;
+    const size_t need = (min == Mem::Host ? ibr : 0) + (mout == Mem::Host ? ob : 0);
+    cudaError_t e = cudaSuccess;
+    const char* where = "kernel launch";
+    if (lane->bounce_cap < need) {
+        if (lane->bounce) cudaFreeHost(lane->bounce);
+        lane->bounce = nullptr;
+        lane->bounce_cap = 0;
+        const size_t cap = need < (64u << 10) ? (64u << 10) : need;
+        e = cudaHostAlloc(&lane->bounce, cap, cudaHostAllocMapped | cudaHostAllocPortable);
+        if (e == cudaSuccess) lane->bounce_cap = cap;
+        else where = "cudaHostAlloc(bounce)";
+    }
+    if (e == cudaSuccess) {
+        char* p = (char*)lane->bounce;
+        const void* din = in;
+        void* dout = out;
+        if (min == Mem::Host) {
+            std::memcpy(p, in, ib);
+            din = p;
+            p += ibr;
+        }
+        if (mout == Mem::Host) dout = p;
+        Slot& sl = lane->slot[0];
+        {
+            ckg::PlainLoadsScope plain;    // page-locked host memory: plain loads, no bulk copies
+            e = enqueue(c, w, w.count, din, dout, nullptr, 0, sl.stream);
+        }
+        const cudaError_t se = cudaStreamSynchronize(sl.stream);
+        if (e == cudaSuccess && se != cudaSuccess) { e = se; where = "cudaStreamSynchronize"; }
+        if (e == cudaSuccess && mout == Mem::Host) std::memcpy(out, dout, ob);
+    }
+    release_lane(c, lane);
+    if (e != cudaSuccess) return cuda_fail(where, e);
+    if (ckg::take_device_error()) return fail("a kernel's bounded wait for its input copy timed out");
+    return 1;
+}
+
 // Runs a request.  stream != NULL with device pointers: asynchronous on that
 // stream.  Mapped page-locked host buffers of single-CTA sizes: one blocking
 // launch in place.  Otherwise blocking, staged through a lane of the
@@ -435,12 +495,14 @@ int run(CkFftContext* c, const Work& w, const void* in, void* out, cudaStream_t 
         (min == Mem::Device || mapped_host(in, (size_t)w.count * w.in_bytes)) &&
         (mout == Mem::Device || mapped_host(out, (size_t)w.count * w.out_bytes)))
         return run_direct(c, w, in, out, min == Mem::Host, user_stream);
+    if (!user_stream && bounce_pays(w, min, mout)) return run_bounce(c, w, in, out, min, mout);
 
     Lane* lane = acquire_lane(c);
     if (!lane) return fail("cannot create a staging lane (CUDA streams)");
     int ok = 1;
     cudaError_t e = cudaSuccess;
     const char* where = "";
+    unsigned used = 0;                    // slot streams this call enqueued work on
     // a user stream orders the blocking call after the stream's earlier work
     cudaEvent_t dep = nullptr;
     if (user_stream) {
@@ -470,7 +532,9 @@ int run(CkFftContext* c, const Work& w, const void* in, void* out, cudaStream_t 
         const bool serial = need != 0;      // shared scratch: keep chunks on one stream
         for (long long off = 0, i = 0; off < w.count; off += chunk, ++i) {
             const long long cnt = (w.count - off < chunk) ? w.count - off : chunk;
-            Slot& sl = lane->slot[serial ? 0 : i % kSlots];
+            const int si = serial ? 0 : (int)(i % kSlots);
+            used |= 1 << si;
+            Slot& sl = lane->slot[si];
             const void* din = (const char*)in + (size_t)off * w.in_bytes;
             void* dout = (char*)out + (size_t)off * w.out_bytes;
             if (min == Mem::Host) {
@@ -498,6 +562,7 @@ int run(CkFftContext* c, const Work& w, const void* in, void* out, cudaStream_t 
     }
 done:
     for (int i = 0; i < kSlots; ++i) {
+        if (!(used >> i & 1)) continue;              // streams this call left idle
         cudaError_t se = cudaStreamSynchronize(lane->slot[i].stream);
         if (e == cudaSuccess && se != cudaSuccess) { e = se; where = "cudaStreamSynchronize"; }
     }
@@ -663,6 +728,41 @@ int run_spans(CkFftContext* c, Span* sp, int nsp, void* stream, Body body)
     const cudaStream_t s = lane->slot[0].stream;
     cudaError_t e = cudaSuccess;
     const char* where = "kernel launch";
+    if (!us && staged && staged <= kBounceMaxBytes) {
+        // small pageable spans: through the lane's page-locked buffer (run_bounce)
+        if (lane->bounce_cap < staged) {
+            if (lane->bounce) cudaFreeHost(lane->bounce);
+            lane->bounce = nullptr;
+            lane->bounce_cap = 0;
+            const size_t cap = staged < (64u << 10) ? (64u << 10) : staged;
+            if ((e = cudaHostAlloc(&lane->bounce, cap, cudaHostAllocMapped | cudaHostAllocPortable)) == cudaSuccess)
+                lane->bounce_cap = cap;
+            else
+                where = "cudaHostAlloc(bounce)";
+        }
+        if (e == cudaSuccess) {
+            char* at = (char*)lane->bounce;
+            for (int i = 0; i < nsp; ++i) {
+                if (!sp[i].staged) continue;
+                sp[i].dev = at;
+                at += (sp[i].span + 255) & ~(size_t)255;
+                // outputs too: the gaps of a strided output keep their contents
+                std::memcpy(sp[i].dev, sp[i].ptr, sp[i].span);
+            }
+            {
+                ckg::PlainLoadsScope plain;
+                e = body(s);
+            }
+            const cudaError_t se = cudaStreamSynchronize(s);
+            if (e == cudaSuccess && se != cudaSuccess) { e = se; where = "cudaStreamSynchronize"; }
+            for (int i = 0; i < nsp && e == cudaSuccess; ++i)
+                if (sp[i].staged && sp[i].output) std::memcpy((void*)sp[i].ptr, sp[i].dev, sp[i].span);
+        }
+        release_lane(c, lane);
+        if (e != cudaSuccess) return cuda_fail(where, e);
+        if (ckg::take_device_error()) return fail("a kernel's bounded wait for its input copy timed out");
+        return 1;
+    }
     cudaEvent_t dep = nullptr;
     void* block = nullptr;
     if (us) {
