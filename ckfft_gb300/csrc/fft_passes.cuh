@@ -11,6 +11,8 @@
 // contiguous bytes.  CG selects L2-only loads (ld.global.cg) for data that
 // another CTA wrote earlier in the same launch.
 #pragma once
+#include <cstdint>
+
 #include "fft_core.cuh"
 
 namespace ckg {
@@ -226,9 +228,25 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
 #pragma unroll
     for (int m = 0; m < P::R; ++m) smem[TileView<P::C>::slot(t + m * P::T, r)] = v[m];
     __syncthreads();
+    if (!live) return;
+    if constexpr (STREAM && P::C % 2 == 0) {
+        if (((uintptr_t)out & 15) == 0) {
+            // two adjacent rows per thread, one 16-byte store each: half the
+            // store instructions (out 16-byte aligned; row0 and r2 even)
+            constexpr int H = P::C / 2, T2 = P::THREADS / H;
+            const int r2 = 2 * (tid % H), t2 = tid / H;
+            float4* dst4 = reinterpret_cast<float4*>(out + row0 + r2);
+#pragma unroll
+            for (int m = 0; m < (1 << LB) / T2; ++m) {
+                const int k2 = t2 + m * T2;
+                const float2 a = smem[TileView<P::C>::slot(k2, r2)], b = smem[TileView<P::C>::slot(k2, r2 + 1)];
+                __stcs(dst4 + (long long)k2 * (n1len / 2), make_float4(a.x, a.y, b.x, b.y));
+            }
+            return;
+        }
+    }
     const int r2 = tid % P::C, t2 = tid / P::C;
     float2* dst = out + row0 + r2;
-    if (!live) return;
 #pragma unroll
     for (int m = 0; m < P::R; ++m) {
         const int k2 = t2 + m * P::T;
