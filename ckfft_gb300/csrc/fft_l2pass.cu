@@ -7,12 +7,13 @@
 // barrier (release / acquire at cluster scope), share the row tiles, and each
 // row tile's CTA drops the intermediate's L2 lines once it has read them.
 // The intermediate of the transforms in flight (resident clusters x 8n
-// bytes, 19 / 38 MB here) stays in the 129 MB L2, so HBM sees the input read
-// once and the output written once -- the traffic of a single pass -- while
-// the batched two-pass kernels move every value through HBM twice.  Measured
-// on GB300 (batches of 1 GiB): 2^15 3328 vs 3145 GB/s, 2^16 3439 vs 3105;
-// the kernel is then bound by the two passes' instructions, not by HBM (40 %
-// DRAM throughput, no intermediate bytes in DRAM).  At 2^17 it was slower
+// bytes, 38 MB at both sizes) stays in the 129 MB L2, so HBM sees the input
+// read once and the output written once -- the traffic of a single pass --
+// while the batched two-pass kernels move every value through HBM twice.
+// Measured on GB300 (batches of 1 GiB): 2^15 3665 GB/s, 2^16 3589, against
+// 3145 / 3105 for the two-pass kernels through HBM; the kernel is bound by
+// the two passes' instructions, not by HBM (41 % DRAM throughput, no
+// intermediate bytes in DRAM).  At 2^17 it was slower
 // (2779 vs 2857) and is not used there.  Real transforms of these half
 // lengths run the batched two-pass kernels with the split / merge fused
 // into a pass instead: a split or merge phase inside this cluster measured
@@ -29,23 +30,26 @@ namespace cg = cooperative_groups;
 namespace ckg {
 
 constexpr int kL2Threads = 256;
-constexpr int kL2Cluster = 8;
 
 template <int LA, int LB>
 struct L2Cfg {
+    // CTAs per transform: 4 at 2^15, 8 at 2^16 (measured on GB300, batches
+    // of 1 GiB: 2^15 3663 GB/s with 4, 3513 with 8, 3474 with 2; 2^16 3591
+    // with 8, 3424 with 4, 3121 with 2)
+    static constexpr int K = LA + LB <= 15 ? 4 : 8;
     using PA = PassCfg<LA, kL2Threads>;
     using PB = PassCfg<LB, kL2Threads>;
     static constexpr int SGA = kL2Threads / PA::THREADS;     // column tiles at once
     static constexpr int SGB = kL2Threads / PB::THREADS;     // row tiles at once
     static constexpr int TILES_A = (1 << LB) / PA::C;        // column tiles of one transform
     static constexpr int TILES_B = (1 << LA) / PB::C;        // row tiles
-    static constexpr int ITER_A = TILES_A / (kL2Cluster * SGA);
-    static constexpr int ITER_B = TILES_B / (kL2Cluster * SGB);
+    static constexpr int ITER_A = TILES_A / (K * SGA);
+    static constexpr int ITER_B = TILES_B / (K * SGB);
     static constexpr size_t SMEM_A = PA::SMEM * SGA, SMEM_B = PB::SMEM * SGB;
     static constexpr size_t SMEM = SMEM_A > SMEM_B ? SMEM_A : SMEM_B;
     static_assert(PA::THREADS * SGA == kL2Threads && PB::THREADS * SGB == kL2Threads, "whole CTAs per phase");
-    static_assert(ITER_A >= 1 && ITER_A * kL2Cluster * SGA == TILES_A, "column tiles split evenly");
-    static_assert(ITER_B >= 1 && ITER_B * kL2Cluster * SGB == TILES_B, "row tiles split evenly");
+    static_assert(ITER_A >= 1 && ITER_A * K * SGA == TILES_A, "column tiles split evenly");
+    static_assert(ITER_B >= 1 && ITER_B * K * SGB == TILES_B, "row tiles split evenly");
 };
 
 __device__ __forceinline__ void cluster_barrier(cg::cluster_group& cluster)
@@ -63,7 +67,7 @@ __device__ __forceinline__ void cluster_barrier(cg::cluster_group& cluster)
 // fr != nullptr: transform f reads fr[f].in and writes fr[f].out (a grouped
 // launch of a job run) instead of in + f in_dist, out + f out_dist.
 template <int LA, int LB, int KIND>
-__global__ void __cluster_dims__(kL2Cluster, 1, 1) __launch_bounds__(kL2Threads, 4)
+__global__ void __cluster_dims__(L2Cfg<LA, LB>::K, 1, 1) __launch_bounds__(kL2Threads, 4)
 k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __restrict__ scratch, long long in_dist,
          long long out_dist, const float2* __restrict__ tw, const FrameDesc* __restrict__ fr)
 {
@@ -72,7 +76,7 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     constexpr long long n = 1ll << (LA + LB);
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
-    const long long f = blockIdx.x / kL2Cluster;
+    const long long f = blockIdx.x / C::K;
     extern __shared__ __align__(128) float2 smem[];
     pdl_start();
     const float2* x = fr ? fr[f].in : in + f * in_dist;
@@ -82,7 +86,7 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     const int sga = threadIdx.x / C::PA::THREADS, ta = threadIdx.x % C::PA::THREADS;
 #pragma unroll 1
     for (int i = 0; i < C::ITER_A; ++i) {
-        const int tile = (i * kL2Cluster + rank) * C::SGA + sga;
+        const int tile = (i * C::K + rank) * C::SGA + sga;
         pass_cols<LA, INV, false, kL2Threads>(x, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
         __syncthreads();                             // the tile's shared memory is reused
     }
@@ -91,7 +95,7 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     const int sgb = threadIdx.x / C::PB::THREADS, tb = threadIdx.x % C::PB::THREADS;
 #pragma unroll 1
     for (int i = 0; i < C::ITER_B; ++i) {
-        const int tile = (i * kL2Cluster + rank) * C::SGB + sgb;
+        const int tile = (i * C::K + rank) * C::SGB + sgb;
         pass_rows<LB, INV, true, kL2Threads, true, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, tw);
         __syncthreads();
     }
@@ -102,7 +106,7 @@ static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, l
                                long long out_dist, const float2* tw, cudaStream_t s, const FrameDesc* fr = nullptr)
 {
     using C = L2Cfg<LA, LB>;
-    return launch_pdl(k_l2_c2c<LA, LB, KIND>, dim3((unsigned)(count * kL2Cluster)), dim3(kL2Threads), C::SMEM, s, in,
+    return launch_pdl(k_l2_c2c<LA, LB, KIND>, dim3((unsigned)(count * C::K)), dim3(kL2Threads), C::SMEM, s, in,
                       out, scratch, in_dist, out_dist, tw, fr);
 }
 
