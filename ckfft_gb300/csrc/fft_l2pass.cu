@@ -93,10 +93,15 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
     // every column tile of the transform is in L2 before any row tile reads it
     cluster_barrier(cluster);
     const int sgb = threadIdx.x / C::PB::THREADS, tb = threadIdx.x % C::PB::THREADS;
+    // the row pass reloads its twiddles: at 2^16 its second stage needs the
+    // same table entries as the column pass's, and keeping those live
+    // across the barrier spills registers
+    const float2* twb = tw;
+    asm volatile("" : "+l"(twb));
 #pragma unroll 1
     for (int i = 0; i < C::ITER_B; ++i) {
         const int tile = (i * C::K + rank) * C::SGB + sgb;
-        pass_rows<LB, INV, true, kL2Threads, true, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, tw);
+        pass_rows_xt<LB, INV, true, kL2Threads, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, twb);
         __syncthreads();
     }
 }

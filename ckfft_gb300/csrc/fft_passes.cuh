@@ -255,6 +255,66 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
     }
 }
 
+// Row pass of rows made of two full-radix stages (LB = 2 log2 R, so T = R
+// threads per row) with the output transpose folded into the stages'
+// exchange.  The first stage runs on thread (r, t) = (tid / T, tid mod T):
+// row r's positions t + mT, coalesced row loads.  Its outputs go to the
+// row's padded shared-memory image; the second stage then runs on thread
+// (r, t) = (tid mod C, tid / C), so the C lanes of one t hold rows row0 ..
+// row0 + C - 1 and each output store covers C consecutive bins k1 of one
+// k2.  One shared-memory round trip per value instead of two (pass_rows
+// exchanges inside the row, then transposes).  Row images are
+// padded_len(N2) = N2 + N2/16 + 1 slots apart, 1 modulo 16: the second
+// stage's reads across rows fall in distinct 8-byte banks, as do the first
+// stage's writes along a row.
+// DISCARD / CG as in pass_rows; outputs are stored with the evict-first hint.
+template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true, int CMAX = 16>
+__device__ __forceinline__ void pass_rows_xt(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
+                                             long long tile, int tid, float2* smem, const float2* __restrict__ tw)
+{
+    using P = PassCfg<LB, MAXT, CMAX>;
+    constexpr int N2 = 1 << LB, R = P::R, T = P::T, LR = P::LOG2R;
+    constexpr int RSTRIDE = padded_len(N2);
+    static_assert(2 * LR == LB && T == R && T % 16 == 0, "two full-radix stages of at least 16");
+    static_assert(RSTRIDE % 16 == 1, "row images one bank apart");
+    const long long n1len = 1ll << log2n1;
+    const long long row0 = tile * P::C;
+    {
+        const int r = tid / T, t = tid % T;
+        const float2* src = in + ((row0 + r) << LB) + t;
+        float2 v[R];
+#pragma unroll
+        for (int m = 0; m < R; ++m) v[m] = ld_data<CG>(src + m * T);
+        stage_compute<LB, LR, LR, 0, INV>(v, t, tw);
+        // outputs to positions tR + j
+        float2* p = smem + r * RSTRIDE + PaddedView::pad(t * R);
+#pragma unroll
+        for (int j = 0; j < R; ++j) p[j + (j >> 4)] = v[j];
+    }
+    __syncthreads();
+    if constexpr (DISCARD) {
+        // every thread of the tile has consumed its inputs: the intermediate
+        // rows are dead, so drop their L2 lines instead of writing them back
+        static_assert(N2 % 16 == 0, "rows span whole 128-byte lines");
+        const char* rows = (const char*)(in + (row0 << LB));
+#pragma unroll
+        for (int l = tid; l < P::C * N2 / 16; l += P::THREADS)
+            asm volatile("discard.global.L2 [%0], 128;" ::"l"(rows + 128 * l) : "memory");
+    }
+    const int r = tid % P::C, t = tid / P::C;
+    const float2* q = smem + r * RSTRIDE + PaddedView::pad(t);
+    float2 v[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) v[m] = q[m * (T + T / 16)];
+    stage_compute<LB, LR, LR, LR, INV>(v, t, tw);
+    // v[j] = X[t + R j] of row row0 + r (32-bit offsets: the transform has
+    // fewer than 2^31 values)
+    float2* dst = out + row0 + r + t * (int)n1len;
+    const int step = R * (int)n1len;
+#pragma unroll
+    for (int j = 0; j < R; ++j) __stcs(dst + j * step, v[j]);
+}
+
 // Row pass of a real forward transform with the split fused (half-length
 // spectrum of M = N1 N2 values, x2 scaling of the reference): tile u holds
 // rows k1 = u C/2 + j and their mirrors N1 - k1 (j < C/2; tile 0 holds row
