@@ -324,19 +324,16 @@ __device__ __forceinline__ void stage_compute_pre(float2 (&v)[1 << LOG2R], const
     });
 }
 
-// Writes a stage's outputs to their Stockham positions, then reloads the
-// thread's registers with positions t + m*T.
-template <int LOG2N, int LOG2R, int LRS, int LNS, bool WARP, int BAR_ID = 0, int BAR_N = 0, class View>
-__device__ __forceinline__ void stage_exchange(float2 (&v)[1 << LOG2R], int t, const View& view)
+// Writes a stage's outputs to their Stockham positions.
+template <int LOG2N, int LOG2R, int LRS, int LNS, class View>
+__device__ __forceinline__ void stage_write(const float2 (&v)[1 << LOG2R], int t, const View& view)
 {
     constexpr int R = 1 << LOG2R, RS = 1 << LRS, NS = 1 << LNS;
     constexpr int T = (1 << LOG2N) / R;
     constexpr int U = R / RS;
-    // With the padded layout, positions base + j*NS and t + m*T map to one
-    // base slot plus compile-time offsets when the span is 1 or a multiple of
-    // 16 (writes) and when T is a multiple of 16 (reads).
+    // With the padded layout, positions base + j*NS map to one base slot plus
+    // compile-time offsets when the span is 1 or a multiple of 16.
     constexpr bool kFastWrite = is_padded<View>() && (NS == 1 || NS % 16 == 0);
-    constexpr bool kFastRead = is_padded<View>() && (T % 16 == 0);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int b = t + u * T;
@@ -353,8 +350,17 @@ __device__ __forceinline__ void stage_exchange(float2 (&v)[1 << LOG2R], int t, c
             for (int j = 0; j < RS; ++j) view.st(base + j * NS, v[u + j * U]);
         }
     }
-    xsync<WARP, BAR_ID, BAR_N>();
-    if constexpr (kFastRead) {
+}
+
+// Loads the thread's registers with positions t + m*T.
+template <int LOG2N, int LOG2R, class View>
+__device__ __forceinline__ void stage_read(float2 (&v)[1 << LOG2R], int t, const View& view)
+{
+    constexpr int R = 1 << LOG2R;
+    constexpr int T = (1 << LOG2N) / R;
+    // padded layout: positions t + m*T are one base slot plus compile-time
+    // offsets when T is a multiple of 16
+    if constexpr (is_padded<View>() && T % 16 == 0) {
         const float2* q = view.base + PaddedView::pad(t);
 #pragma unroll
         for (int m = 0; m < R; ++m) v[m] = q[m * (T + T / 16)];
@@ -362,6 +368,16 @@ __device__ __forceinline__ void stage_exchange(float2 (&v)[1 << LOG2R], int t, c
 #pragma unroll
         for (int m = 0; m < R; ++m) v[m] = view.ld(t + m * T);
     }
+}
+
+// Writes a stage's outputs to their Stockham positions, then reloads the
+// thread's registers with positions t + m*T.
+template <int LOG2N, int LOG2R, int LRS, int LNS, bool WARP, int BAR_ID = 0, int BAR_N = 0, class View>
+__device__ __forceinline__ void stage_exchange(float2 (&v)[1 << LOG2R], int t, const View& view)
+{
+    stage_write<LOG2N, LOG2R, LRS, LNS>(v, t, view);
+    xsync<WARP, BAR_ID, BAR_N>();
+    stage_read<LOG2N, LOG2R>(v, t, view);
     xsync<WARP, BAR_ID, BAR_N>();
 }
 

@@ -73,7 +73,7 @@ k_rows(const float2* __restrict__ in, float2* __restrict__ out, long long count,
     pdl_start();
     const long long tiles = (1ll << log2n1) / P::C;
     const long long f = blockIdx.x / tiles;
-    pass_rows<LB, INV, false, BatchMaxT<LB>::value, true, true, BatchCMax<LB>::value>(
+    pass_rows_xt<LB, INV, false, BatchMaxT<LB>::value, true, BatchCMax<LB>::value>(
         in + f * in_dist, out + f * out_dist, log2n1, blockIdx.x % tiles, threadIdx.x, smem, tw);
 }
 
@@ -95,8 +95,8 @@ k_rows3(const float2* __restrict__ in, float2* __restrict__ out, int l1, int l2,
     const long long k2 = (b / tiles) & ((1ll << l2) - 1);
     const long long f = b / (tiles << l2);
     const long long n = 1ll << (l1 + l2 + LB);
-    pass_rows<LB, INV, false, BatchMaxT<LB>::value, true, true, BatchCMax<LB>::value>(
-        in + f * n + (k2 << LB), out + f * out_dist + (k2 << l1), l1 + l2, tile, threadIdx.x, smem, tw, true, l2 + LB);
+    pass_rows_xt<LB, INV, false, BatchMaxT<LB>::value, true, BatchCMax<LB>::value>(
+        in + f * n + (k2 << LB), out + f * out_dist + (k2 << l1), l1 + l2, tile, threadIdx.x, smem, tw, l2 + LB);
 }
 
 // Row pass of a real forward transform with the split fused: block
@@ -185,7 +185,7 @@ k_rows_inv_table(const float2* __restrict__ tmp, const FrameDesc* __restrict__ f
     pdl_start();
     const long long tiles = (1ll << log2n1) / P::C;
     const long long f = blockIdx.x / tiles;
-    pass_rows<LB, true, false, BatchMaxT<LB>::value, true, true, BatchCMax<LB>::value>(
+    pass_rows_xt<LB, true, false, BatchMaxT<LB>::value, true, BatchCMax<LB>::value>(
         tmp + (f << (log2n1 + LB)), fr[f].out, log2n1, blockIdx.x % tiles, threadIdx.x, smem, tw);
 }
 

@@ -255,64 +255,72 @@ __device__ __forceinline__ void pass_rows(const float2* __restrict__ in, float2*
     }
 }
 
-// Row pass of rows made of two full-radix stages (LB = 2 log2 R, so T = R
-// threads per row) with the output transpose folded into the stages'
-// exchange.  The first stage runs on thread (r, t) = (tid / T, tid mod T):
-// row r's positions t + mT, coalesced row loads.  Its outputs go to the
-// row's padded shared-memory image; the second stage then runs on thread
+// Row pass with the output transpose folded into the last stage exchange.
+// All stages but the last run on thread (r, t) = (tid / T, tid mod T): row
+// r's positions t + mT, coalesced row loads, exchanges inside the row as in
+// pass_rows.  The second-to-last stage writes its outputs to the row's
+// padded shared-memory image; the last stage then runs on thread
 // (r, t) = (tid mod C, tid / C), so the C lanes of one t hold rows row0 ..
 // row0 + C - 1 and each output store covers C consecutive bins k1 of one
-// k2.  One shared-memory round trip per value instead of two (pass_rows
-// exchanges inside the row, then transposes).  Row images are
-// padded_len(N2) = N2 + N2/16 + 1 slots apart, 1 modulo 16: the second
-// stage's reads across rows fall in distinct 8-byte banks, as do the first
-// stage's writes along a row.
-// DISCARD / CG as in pass_rows; outputs are stored with the evict-first hint.
+// k2.  One shared-memory round trip per value fewer than pass_rows
+// (exchange inside the row, then a transpose).  Row images are
+// padded_len(N2) slots apart, an odd number: the last stage's reads across
+// 16 rows fall in distinct 8-byte banks.
+// DISCARD / CG / log2_row_stride as in pass_rows; outputs are stored with
+// the evict-first hint.
 template <int LB, bool INV, bool CG, int MAXT = 512, bool DISCARD = true, int CMAX = 16>
 __device__ __forceinline__ void pass_rows_xt(const float2* __restrict__ in, float2* __restrict__ out, int log2n1,
-                                             long long tile, int tid, float2* smem, const float2* __restrict__ tw)
+                                             long long tile, int tid, float2* smem, const float2* __restrict__ tw,
+                                             int log2_row_stride = LB)
 {
     using P = PassCfg<LB, MAXT, CMAX>;
-    constexpr int N2 = 1 << LB, R = P::R, T = P::T, LR = P::LOG2R;
+    using S = Sched<LB, P::LOG2R>;
+    constexpr int N2 = 1 << LB, R = P::R, T = P::T, LR = P::LOG2R, NST = S::nstages;
     constexpr int RSTRIDE = padded_len(N2);
-    static_assert(2 * LR == LB && T == R && T % 16 == 0, "two full-radix stages of at least 16");
-    static_assert(RSTRIDE % 16 == 1, "row images one bank apart");
+    static_assert(NST >= 2, "at least two stages");
+    static_assert(RSTRIDE % 2 == 1 && P::C * RSTRIDE <= P::SLOTS, "odd row stride inside the tile's memory");
     const long long n1len = 1ll << log2n1;
     const long long row0 = tile * P::C;
+    const long long rstride = 1ll << log2_row_stride;
+    float2 v[R];
     {
         const int r = tid / T, t = tid % T;
-        const float2* src = in + ((row0 + r) << LB) + t;
-        float2 v[R];
+        const float2* src = in + (row0 + r) * rstride + t;
 #pragma unroll
         for (int m = 0; m < R; ++m) v[m] = ld_data<CG>(src + m * T);
-        stage_compute<LB, LR, LR, 0, INV>(v, t, tw);
-        // outputs to positions tR + j
-        float2* p = smem + r * RSTRIDE + PaddedView::pad(t * R);
-#pragma unroll
-        for (int j = 0; j < R; ++j) p[j + (j >> 4)] = v[j];
+        PaddedView view{smem + r * RSTRIDE};
+        static_for<0, NST - 1>([&](auto sc) {
+            constexpr int st = decltype(sc)::value;
+            stage_compute<LB, LR, S::lrs(st), S::lns(st), INV>(v, t, tw);
+            if constexpr (st + 2 < NST) stage_exchange<LB, LR, S::lrs(st), S::lns(st), (T <= 32)>(v, t, view);
+            else stage_write<LB, LR, S::lrs(st), S::lns(st)>(v, t, view);
+        });
     }
     __syncthreads();
     if constexpr (DISCARD) {
         // every thread of the tile has consumed its inputs: the intermediate
         // rows are dead, so drop their L2 lines instead of writing them back
         static_assert(N2 % 16 == 0, "rows span whole 128-byte lines");
-        const char* rows = (const char*)(in + (row0 << LB));
+        constexpr int LINES = N2 / 16;
 #pragma unroll
-        for (int l = tid; l < P::C * N2 / 16; l += P::THREADS)
-            asm volatile("discard.global.L2 [%0], 128;" ::"l"(rows + 128 * l) : "memory");
+        for (int l = tid; l < P::C * LINES; l += P::THREADS) {
+            const char* row = (const char*)(in + (row0 + l / LINES) * rstride);
+            asm volatile("discard.global.L2 [%0], 128;" ::"l"(row + 128 * (l % LINES)) : "memory");
+        }
     }
     const int r = tid % P::C, t = tid / P::C;
-    const float2* q = smem + r * RSTRIDE + PaddedView::pad(t);
-    float2 v[R];
-#pragma unroll
-    for (int m = 0; m < R; ++m) v[m] = q[m * (T + T / 16)];
-    stage_compute<LB, LR, LR, LR, INV>(v, t, tw);
-    // v[j] = X[t + R j] of row row0 + r (32-bit offsets: the transform has
-    // fewer than 2^31 values)
+    stage_read<LB, LR>(v, t, PaddedView{smem + r * RSTRIDE});
+    constexpr int LRS = S::lrs(NST - 1), LNS = S::lns(NST - 1);
+    stage_compute<LB, LR, LRS, LNS, INV>(v, t, tw);
+    // v[u + j U] = X[t + u T + j NS] of row row0 + r (the last stage's span
+    // NS = N2 / RS; 32-bit offsets: the transform has fewer than 2^31 values)
+    constexpr int U = R >> LRS, NS = 1 << LNS;
     float2* dst = out + row0 + r + t * (int)n1len;
-    const int step = R * (int)n1len;
 #pragma unroll
-    for (int j = 0; j < R; ++j) __stcs(dst + j * step, v[j]);
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+        for (int j = 0; j < (1 << LRS); ++j) __stcs(dst + (u * T + j * NS) * (int)n1len, v[u + j * U]);
+    }
 }
 
 // Row pass of a real forward transform with the split fused (half-length
