@@ -114,8 +114,8 @@ __device__ __noinline__ void run_pass(const UnitRec& r, const JobsArgs& a, float
     const long long tile = (long long)u.first + s;
     if constexpr (OP == U_COLS_FWD) pass_cols<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
     else if constexpr (OP == U_COLS_INV) pass_cols<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
-    else if constexpr (OP == U_ROWS_FWD) pass_rows<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
-    else if constexpr (OP == U_ROWS_INV) pass_rows<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_ROWS_FWD) pass_rows_xt<LS, false, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
+    else if constexpr (OP == U_ROWS_INV) pass_rows_xt<LS, true, true, kJobThreads>(src, dst, u.log2b, tile, tid, my, a.tw);
     else if constexpr (OP == U_COLS_MERGE)
         pass_cols_merge<LS, kJobThreads, 16, true>(src, dst, u.log2b, tile, tid, my, a.tw);
     else pass_rows_split<LS, kJobThreads, true>(src, dst, u.log2b, tile, tid, my, a.tw, u.log2b);
