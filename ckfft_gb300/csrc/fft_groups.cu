@@ -3,9 +3,10 @@
 // hardware-scheduled launch that reads each transform's input and output
 // pointers from a table (FrameDesc), instead of as units of the persistent
 // kernel.  The frame bodies are the batched kernels' (fft_small.cuh); the
-// 2^15 / 2^16 complex groups use the cluster two-pass kernel with its table
-// argument (fft_l2pass.cu), real 2^16 / 2^17 the two-pass kernels with the
-// split / merge fused (fft_large.cu).
+// 2^15 / 2^16 complex groups and the real 2^16 / 2^17 groups use the
+// cluster two-pass kernel with its table argument (fft_l2pass.cu; real: the
+// split / merge fused into its tiles).  The fused two-pass table kernels of
+// fft_large.cu stay for a build that takes the real kinds off that kernel.
 #include "fft_small.cuh"
 #include "jobs.h"
 #include "kernels.h"
@@ -80,8 +81,8 @@ static cudaError_t launch_table(int l, const FrameDesc* fr, long long count, con
 
 // Sizes the job kernel runs as two phases of pass units (log2a above
 // kJobMaxSingleLog2) and a batched kernel runs in one launch: single-CTA up
-// to 2^14, the cluster two-pass kernel at 2^15 / 2^16 (complex), two passes
-// with the split / merge fused at 2^15 / 2^16 (real).
+// to 2^14, the cluster two-pass kernel at 2^15 / 2^16 (complex, and real
+// half lengths with the split / merge fused).
 bool group_supported(int op, int log2a)
 {
     if (log2a <= kJobMaxSingleLog2) return false;
@@ -105,6 +106,10 @@ cudaError_t launch_group(int op, int log2a, const FrameDesc* fr, long long count
                          void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
     if (count <= 0) return cudaSuccess;
+    if (log2a > 14 && op == U_R2C && l2pass_supported(log2a) && l2pass_real(2))
+        return launch_l2pass_table(2, log2a, fr, count, tw, scratch, scratch_bytes, s);
+    if (log2a > 14 && op == U_C2R && l2pass_supported(log2a) && l2pass_real(3))
+        return launch_l2pass_table(3, log2a, fr, count, tw, scratch, scratch_bytes, s);
     if (log2a > 14 && op == U_R2C) return launch_r2c_table(log2a, fr, count, tw, scratch, scratch_bytes, s);
     if (log2a > 14 && op == U_C2R) return launch_c2r_table(log2a, fr, count, tw, scratch, scratch_bytes, s);
     if (log2a > 14) {

@@ -10,15 +10,15 @@
 // bytes, 38 MB at both sizes) stays in the 129 MB L2, so HBM sees the input
 // read once and the output written once -- the traffic of a single pass --
 // while the batched two-pass kernels move every value through HBM twice.
-// Measured on GB300 (batches of 1 GiB): 2^15 3665 GB/s, 2^16 3589, against
+// Measured on GB300 (batches of 1 GiB): 2^15 3929 GB/s, 2^16 3851, against
 // 3145 / 3105 for the two-pass kernels through HBM; the kernel is bound by
-// the two passes' instructions, not by HBM (41 % DRAM throughput, no
-// intermediate bytes in DRAM).  At 2^17 it was slower
-// (2779 vs 2857) and is not used there.  Real transforms of these half
-// lengths run the batched two-pass kernels with the split / merge fused
-// into a pass instead: a split or merge phase inside this cluster measured
-// slower (real 2^16 forward 2109 against 2550 GB/s, inverse 2262 against
-// 2607).
+// the two passes' instructions, not by HBM (43 % DRAM throughput, no
+// intermediate bytes in DRAM).  At 2^17 it was slower (2779 vs 2857) and is
+// not used there.  Real transforms of 2^16 / 2^17 points (these half
+// lengths) run here too, the split fused into the row tiles and the merge
+// into the column tiles (pass_rows_split, pass_cols_merge): forward 2593 /
+// 2621 GB/s, inverse 2780 / 2656, against 2507 / 2609 and 2714 / 2554 for
+// the same fused passes through HBM.
 #include <cooperative_groups.h>
 
 #include "fft_passes.cuh"
@@ -64,6 +64,10 @@ __device__ __forceinline__ void cluster_barrier(cg::cluster_group& cluster)
 // One transform per cluster: blockIdx.x / K.  scratch holds 2^(LA+LB) values
 // per transform of the launch (128-byte aligned rows).
 // KIND 0 / 1: complex forward / inverse of n = 2^(LA+LB) points.
+// KIND 2: real forward of 2n reals (read as n packed complex values) to
+// n + 1 bins, the split fused into the row tiles (pass_rows_split).
+// KIND 3: real inverse of n + 1 bins to 2n reals, the merge fused into the
+// column tiles (pass_cols_merge).
 // fr != nullptr: transform f reads fr[f].in and writes fr[f].out (a grouped
 // launch of a job run) instead of in + f in_dist, out + f out_dist.
 template <int LA, int LB, int KIND>
@@ -72,7 +76,7 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
          long long out_dist, const float2* __restrict__ tw, const FrameDesc* __restrict__ fr)
 {
     using C = L2Cfg<LA, LB>;
-    constexpr bool INV = KIND == 1;
+    constexpr bool INV = KIND == 1 || KIND == 3;
     constexpr long long n = 1ll << (LA + LB);
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
@@ -87,7 +91,8 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
 #pragma unroll 1
     for (int i = 0; i < C::ITER_A; ++i) {
         const int tile = (i * C::K + rank) * C::SGA + sga;
-        pass_cols<LA, INV, false, kL2Threads>(x, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
+        if constexpr (KIND == 3) pass_cols_merge<LA, kL2Threads>(x, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
+        else pass_cols<LA, INV, false, kL2Threads>(x, s, LB, tile, ta, smem + sga * C::PA::SLOTS, tw);
         __syncthreads();                             // the tile's shared memory is reused
     }
     // every column tile of the transform is in L2 before any row tile reads it
@@ -101,7 +106,9 @@ k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __rest
 #pragma unroll 1
     for (int i = 0; i < C::ITER_B; ++i) {
         const int tile = (i * C::K + rank) * C::SGB + sgb;
-        pass_rows_xt<LB, INV, true, kL2Threads, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, twb);
+        if constexpr (KIND == 2)
+            pass_rows_split<LB, kL2Threads, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, twb, LA);
+        else pass_rows_xt<LB, INV, true, kL2Threads, true>(s, y, LA, tile, tb, smem + sgb * C::PB::SLOTS, twb);
         __syncthreads();
     }
 }
@@ -117,11 +124,17 @@ static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, l
 
 bool l2pass_supported(int log2n) { return log2n >= 15 && log2n <= 16; }
 
-// kind: 0 / 1 complex forward / inverse (dists in complex units).
+// Real kinds on this kernel (bit 0: forward, bit 1: inverse).
+constexpr int kL2Real = 3;
+
+bool l2pass_real(int kind) { return (kind == 2 && (kL2Real & 1)) || (kind == 3 && (kL2Real & 2)); }
+
+// kind: 0 / 1 complex forward / inverse, 2 / 3 real forward / inverse of
+// 2^(log2n+1) reals (log2n: the complex half length); dists in complex units.
 cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,
                           long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
-    if (!l2pass_supported(log2n) || (kind != 0 && kind != 1)) return cudaErrorInvalidValue;
+    if (!l2pass_supported(log2n) || kind < 0 || kind > 3) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;
     const long long n = 1ll << log2n;
     const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
@@ -137,7 +150,9 @@ cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long l
 #define CKG_L2_KIND(LA, LB)                                                                        \
     switch (kind) {                                                                                \
     case 0: e = launch_l2_L<LA, LB, 0>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
-    default: e = launch_l2_L<LA, LB, 1>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;          \
+    case 1: e = launch_l2_L<LA, LB, 1>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
+    case 2: e = launch_l2_L<LA, LB, 2>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;           \
+    default: e = launch_l2_L<LA, LB, 3>(a, b, tmp, cnt, in_dist, out_dist, tw, s); break;          \
     }
         if (log2n == 15) { CKG_L2_KIND(7, 8) }
         else { CKG_L2_KIND(8, 8) }
@@ -152,7 +167,7 @@ cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long l
 cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
                                 void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
-    if (!l2pass_supported(log2n) || (kind != 0 && kind != 1)) return cudaErrorInvalidValue;
+    if (!l2pass_supported(log2n) || kind < 0 || kind > 3) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;
     const long long n = 1ll << log2n;
     const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)n));
@@ -165,7 +180,9 @@ cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long l
 #define CKG_L2_KIND(LA, LB)                                                                              \
     switch (kind) {                                                                                      \
     case 0: e = launch_l2_L<LA, LB, 0>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;               \
-    default: e = launch_l2_L<LA, LB, 1>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;              \
+    case 1: e = launch_l2_L<LA, LB, 1>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;               \
+    case 2: e = launch_l2_L<LA, LB, 2>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;               \
+    default: e = launch_l2_L<LA, LB, 3>(nullptr, nullptr, tmp, cnt, 0, 0, tw, s, g); break;              \
     }
         if (log2n == 15) { CKG_L2_KIND(7, 8) }
         else { CKG_L2_KIND(8, 8) }
@@ -183,6 +200,8 @@ static cudaError_t attr_l2()
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 0>, a, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 1>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 2>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_l2_c2c<LA, LB, 3>, a, smem);
     return e;
 }
 

@@ -531,12 +531,14 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
                              void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
     // in: n floats per frame (n/2 packed complex), out: n/2+1 complex per frame
-    // (half lengths 2^15 / 2^16 too: the fused two-pass form measured faster
-    // than a cluster kernel with the intermediate in L2 and a split phase,
-    // 2550 vs 2109 GB/s batched at n = 2^16)
+    // (half lengths 2^15 / 2^16: the cluster kernel with the split fused into
+    // its row tiles, 2593 / 2621 GB/s batched at n = 2^16 / 2^17 against 2507
+    // / 2609 for the fused two-pass form through HBM)
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
     if (count <= 0) return cudaSuccess;
+    if (l2pass_supported(lm) && l2pass_real(2) && ((uintptr_t)scratch & 127) == 0)
+        return launch_l2pass(2, lm, in, out, count, in_dist / 2, out_dist, tw, scratch, scratch_bytes, s);
     if (rows_split_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_r2c_rows_split(lm, (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw,
                                      (float2*)scratch, scratch_bytes, s);
@@ -614,12 +616,14 @@ cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long cou
                              void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
     // in: n/2+1 complex per frame, out: n floats per frame (n/2 packed complex)
-    // (half lengths 2^15 / 2^16 too: the merge fused into the column pass
-    // measured 2607 / 2454 GB/s against 2262 / 2439 for the cluster kernel
-    // with a merge phase)
+    // (half lengths 2^15 / 2^16: the cluster kernel with the merge fused into
+    // its column tiles, 2780 / 2656 GB/s batched at n = 2^16 / 2^17 against
+    // 2714 / 2554 for the fused two-pass form through HBM)
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
     if (count <= 0) return cudaSuccess;
+    if (l2pass_supported(lm) && l2pass_real(3) && ((uintptr_t)scratch & 127) == 0)
+        return launch_l2pass(3, lm, in, out, count, in_dist, out_dist / 2, tw, scratch, scratch_bytes, s);
     if (cols_merge_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_c2r_cols_merge(lm, (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw,
                                      (float2*)scratch, scratch_bytes, s);

@@ -107,9 +107,11 @@ cudaError_t launch_cluster_c2c(bool inverse, int log2n, const void* in, void* ou
 // Complex 2^15 and 2^16 with both passes inside one thread-block cluster per
 // transform and the intermediate kept in L2 (fft_l2pass.cu); scratch as for
 // launch_large_c2c, 128-byte aligned.
-// kind: 0 / 1 complex forward / inverse of 2^log2n points (dists in complex
-// units).
+// kind: 0 / 1 complex forward / inverse of 2^log2n points, 2 / 3 real
+// forward / inverse of 2^(log2n+1) points (split / merge fused; dists in
+// complex units).  l2pass_real(kind): the real kind runs on this kernel.
 bool l2pass_supported(int log2n);
+bool l2pass_real(int kind);
 cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,
                           long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes,
                           cudaStream_t stream);

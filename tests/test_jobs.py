@@ -143,9 +143,9 @@ def test_plan_replays_and_reads_current_inputs(torch_cuda, ctx_cache, oracle_mod
 def test_plan_groups_multi_pass_sizes(torch_cuda, ctx_cache, oracle_mod):
     """Transforms the job kernel would split into pass units run as grouped
     launches over pointer tables (single-CTA tables at complex 2^13 / real
-    2^15, the cluster kernel at complex 2^15, the fused two-pass real forward
-    and inverse at 2^16), beside the persistent kernel that takes the small
-    ones: one replay launches exactly those kernels."""
+    2^15, the cluster kernel at complex 2^15 and for the real forward and
+    inverse at 2^16, split / merge fused), beside the persistent kernel that
+    takes the small ones: one replay launches exactly those kernels."""
     from ckfft_gb300 import binding
     torch = torch_cuda
     rng = np.random.default_rng(5)
@@ -156,8 +156,8 @@ def test_plan_groups_multi_pass_sizes(torch_cuda, ctx_cache, oracle_mod):
     plan = ctx.plan([as_tuple(j) for j in jobs])
     before = binding.launch_count()
     ctx.check(plan.exec(), "exec")
-    # 2 single-CTA tables + 1 cluster launch + 2 x 2 passes (real 2^16) + the job kernel
-    assert binding.launch_count() - before == 8
+    # 2 single-CTA tables + 3 cluster launches (complex 2^15, real 2^16 both ways) + the job kernel
+    assert binding.launch_count() - before == 6
     o = oracle_mod.Oracle(1 << 16)
     for j in jobs:
         got = j["out"].cpu().numpy()
