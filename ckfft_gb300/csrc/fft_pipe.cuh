@@ -130,6 +130,153 @@ k_pipe(const float2* __restrict__ in, float2* __restrict__ out, long long ngroup
     }
 }
 
+// ------------------------------------------------ split-exchange form
+// Complex frames too large for one buffer to be both the landing zone and
+// the exchange area twice over (2^14: 128 KiB a frame) keep the two apart:
+// one landing buffer the size of a group, and an exchange area that moves
+// the x parts, then the y parts, through a float image padded every 32
+// elements (68 KiB at 2^14; 196 KiB a CTA in all).  The copy of the next
+// group is issued as soon as every thread holds its inputs, so it lands
+// while this group's stages and stores run.  Same stages, twiddles and
+// positions as the other forms: the same results bit for bit.
+template <int L, int KIND>
+struct PipeSxCfg {
+    using C = SmallCfg<L>;
+    static constexpr int N = 1 << L;
+    static constexpr unsigned GROUP_BYTES = (unsigned)(C::TPB * N * sizeof(float2));
+    static constexpr int LAND = C::TPB * N;                          // float2
+    static constexpr int XLEN = N + (N >> 5) + 1;                    // floats per frame image
+    static constexpr int XBUF = (C::TPB * XLEN + 3) / 4 * 4;         // floats (16-byte multiple)
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)LAND + sizeof(float) * (size_t)XBUF;
+    static constexpr bool FITS = (KIND == C2C_FWD || KIND == C2C_INV) && !PipeCfg<L, KIND, 2>::FITS &&
+                                 SMEM <= 227 * 1024 && C::T % 32 == 0;
+};
+
+__device__ __forceinline__ int pad32(int pos) { return pos + (pos >> 5); }
+
+// One exchange of a stage's outputs through the float image xa: every thread
+// writes the x parts of its outputs to their Stockham positions and reloads
+// the x parts of positions t + mT, then the same for the y parts.
+template <int LOG2N, int LOG2R, int LRS, int LNS, bool WARP>
+__device__ __forceinline__ void exchange_split(float2 (&v)[1 << LOG2R], int t, float* xa)
+{
+    constexpr int R = 1 << LOG2R, RS = 1 << LRS, NS = 1 << LNS;
+    constexpr int T = (1 << LOG2N) / R, U = R / RS;
+    static_assert(T % 32 == 0 && RS <= 32 && (NS == 1 || NS % 32 == 0), "compile-time image offsets");
+    static_for<0, 2>([&](auto cc) {
+        constexpr int comp = decltype(cc)::value;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int b = t + u * T;
+            const int base = ((b >> LNS) << (LNS + LRS)) + (b & (NS - 1));
+            // base + j NS -> pad32(base) + j (NS == 1, base a multiple of
+            // RS <= 32 ... here of 32 when RS = 32) or + j (NS + NS / 32)
+            float* p = xa + pad32(base);
+#pragma unroll
+            for (int j = 0; j < RS; ++j) {
+                const int off = NS == 1 ? j : j * (NS + NS / 32);
+                p[off] = comp ? v[u + j * U].y : v[u + j * U].x;
+            }
+        }
+        xsync<WARP>();
+        const float* q = xa + pad32(t);
+#pragma unroll
+        for (int m = 0; m < R; ++m) {
+            const float f = q[m * (T + T / 32)];
+            if constexpr (comp) v[m].y = f;
+            else v[m].x = f;
+        }
+        xsync<WARP>();
+    });
+}
+
+template <int LOG2N, int LOG2R, bool INV, bool WARP>
+__device__ __forceinline__ void stockham_split(float2 (&v)[1 << LOG2R], int t, const float2* __restrict__ tw, float* xa)
+{
+    using S = Sched<LOG2N, LOG2R>;
+    static_for<0, S::nstages>([&](auto sc) {
+        constexpr int st = decltype(sc)::value;
+        stage_compute<LOG2N, LOG2R, S::lrs(st), S::lns(st), INV>(v, t, tw);
+        if constexpr (st + 1 < S::nstages) exchange_split<LOG2N, LOG2R, S::lrs(st), S::lns(st), WARP>(v, t, xa);
+    });
+}
+
+template <int L, int KIND>
+__global__ void __launch_bounds__(SmallCfg<L>::THREADS, SmallCfg<L>::MINB)
+k_pipe_sx(const float2* __restrict__ in, float2* __restrict__ out, long long ngroups, long long out_dist,
+          const float2* __restrict__ tw, unsigned* err)
+{
+    using P = PipeSxCfg<L, KIND>;
+    using C = SmallCfg<L>;
+    constexpr int N = P::N;
+    constexpr bool INV = KIND == C2C_INV;
+    extern __shared__ __align__(128) float2 smem[];
+    __shared__ __align__(8) unsigned long long bar;
+    float* xa = reinterpret_cast<float*>(smem + P::LAND);
+    const int g = threadIdx.x / C::T, t = threadIdx.x % C::T;
+    const uint32_t b = smem_addr(&bar);
+    pdl_start();
+    if (threadIdx.x == 0) {
+        mbar_init(b, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](long long grp) {
+        mbar_arrive_expect_tx(b, P::GROUP_BYTES);
+        bulk_load(smem_addr(smem), in + grp * (long long)P::LAND, P::GROUP_BYTES, b);
+    };
+    if (threadIdx.x == 0 && (long long)blockIdx.x < ngroups) issue(blockIdx.x);
+
+    long long failed_at = -1;
+    for (long long i = 0;; ++i) {
+        const long long grp = blockIdx.x + i * gridDim.x;
+        if (grp >= ngroups) break;
+        const bool ok = mbar_wait(b, (uint32_t)(i & 1), err);
+        const float2* land = smem + g * N;
+        float2 v[C::R];
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) v[m] = land[t + m * C::T];
+        // every input is in registers before the next copy overwrites the
+        // landing zone; a timed-out wait anywhere stops the whole CTA
+        if (__syncthreads_or(!ok)) { failed_at = i; break; }
+        if (threadIdx.x == 0) {
+            const long long next = grp + gridDim.x;
+            if (next < ngroups) {
+                fence_proxy_async_shared();
+                issue(next);
+            }
+        }
+        stockham_split<L, C::LOG2R, INV, C::WARP>(v, t, tw, xa + g * P::XLEN);
+        float2* dst = out + (grp * C::TPB + g) * out_dist + t;
+#pragma unroll
+        for (int m = 0; m < C::R; ++m) __stcs(dst + m * C::T, v[m]);
+    }
+    if (failed_at >= 0 && threadIdx.x == 0) {
+        // the copy of iteration failed_at may still be in flight: give it a
+        // bounded chance to land before the CTA exits
+        for (int it = 0; it < 4096 && !mbar_try_wait(b, (uint32_t)(failed_at & 1)); ++it) {
+        }
+    }
+}
+
+template <int L, int KIND>
+int pipe_sx_grid(long long ngroups)
+{
+    using P = PipeSxCfg<L, KIND>;
+    static int per_sm = -1, sms = 0;
+    if (per_sm < 0) {
+        int dev = 0, nb = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pipe_sx<L, KIND>, SmallCfg<L>::THREADS, P::SMEM) !=
+            cudaSuccess)
+            nb = 1;
+        per_sm = nb > 0 ? nb : 1;
+    }
+    const long long cap = (long long)per_sm * sms;
+    return (int)(ngroups < cap ? ngroups : cap);
+}
+
 // Resident CTAs per SM for a pipelined kernel (cached per instantiation).
 template <int L, int KIND, int NBUF>
 int pipe_grid(long long ngroups)
@@ -153,6 +300,13 @@ cudaError_t attr_pipe()
 {
     using P = PipeCfg<L, KIND, NBUF>;
     if constexpr (!P::FITS) {
+        using X = PipeSxCfg<L, KIND>;
+        if constexpr (X::FITS) {
+            cudaError_t e = cudaFuncSetAttribute(k_pipe_sx<L, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)X::SMEM);
+            if (e != cudaSuccess) return e;
+            return cudaFuncSetAttribute(k_pipe_sx<L, KIND>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        }
         return cudaSuccess;
     } else {
         cudaError_t e = cudaFuncSetAttribute(k_pipe<L, KIND, NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM);
@@ -171,6 +325,18 @@ cudaError_t launch_pipe(const void* in, void* out, long long count, long long in
     using C = SmallCfg<L>;
     *done = 0;
     if constexpr (!P::FITS) {
+        // the split-exchange form, one landing buffer whatever NBUF asks
+        using X = PipeSxCfg<L, KIND>;
+        if constexpr (X::FITS) {
+            const long long ngroups = count / C::TPB;
+            if (ngroups < 1 || in_dist != X::N || ((uintptr_t)in & 15) || (X::GROUP_BYTES & 15) || !err)
+                return cudaSuccess;
+            const int grid = pipe_sx_grid<L, KIND>(ngroups);
+            const cudaError_t e = launch_pdl(k_pipe_sx<L, KIND>, dim3(grid), dim3(C::THREADS), X::SMEM, s,
+                                             (const float2*)in, (float2*)out, ngroups, out_dist, tw, err);
+            *done = ngroups * C::TPB;
+            return e;
+        }
         return cudaSuccess;
     } else {
         const long long ngroups = count / C::TPB;

@@ -11,8 +11,8 @@
 namespace ckg {
 constexpr signed char kTunedLog2R[15] = {0, 1, 2, 3, 4, 4, 3, 3, 4, 4, 4, 4, 4, 5, 5};
 constexpr signed char kTunedVariant[4][15] = {
-    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 7, 7, 0, 0, 0},   // cfwd
-    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 7, 7, 0, 0, 0},   // cinv
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 7, 7, 0, 0, 2},   // cfwd
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 7, 7, 0, 0, 2},   // cinv
     {0, 0, 0, 0, 0, 0, 0, 7, 0, 7, 7, 7, 0, 0, 0},   // rfwd
     {0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 2, 2, 0, 0, 0},   // rinv
 };
