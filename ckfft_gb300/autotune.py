@@ -10,7 +10,10 @@ Variants (the dimensions searched):
   2, 3 persistent kernel with 2 / 3 bulk-copy (TMA) buffers, default shape;
   4, 5 half / twice the values per thread (radix 8 / 32 stages: threads per
        transform x2 / x0.5, so the radix order changes with it);
-  6, 7 transforms per CTA filling 512 / 128 threads.
+  6, 7 transforms per CTA filling 512 / 128 threads;
+  8    persistent kernel with one bulk-copy landing buffer and a separate
+       exchange area that moves the x parts, then the y parts (complex kinds;
+       the form that fits complex 2^14).
 Each variant is measured in its own process (the library reads
 CKFFT_CUDA_VARIANT once), on batches of about --mb MiB of input per launch,
 with CUDA events around --reps launches after warm-up; a variant that does not
@@ -37,8 +40,8 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 KINDS = ["cfwd", "cinv", "rfwd", "rinv"]   # index = ckg::Kind
-VARIANTS = [0, 2, 3, 4, 5, 6, 7]
-NAMES = ["plain", "pipe x2", "pipe x3", "R/2", "2R", "512 thr", "128 thr"]
+VARIANTS = [0, 2, 3, 4, 5, 6, 7, 8]
+NAMES = ["plain", "pipe x2", "pipe x3", "R/2", "2R", "512 thr", "128 thr", "pipe sx"]
 LOG2_RANGE = range(0, 15)                  # complex (half) length 2^L
 
 
@@ -96,7 +99,7 @@ def current_log2r() -> list:
 
 # Variants that keep a frame's arithmetic (same radices, so the same bits as
 # every other kernel family of the size): pipelined loads, CTA size.
-SAME_BITS = [2, 3, 6, 7]
+SAME_BITS = [2, 3, 6, 7, 8]
 
 
 def choose(results: dict, lr0: list):
@@ -138,8 +141,9 @@ def write_outputs(results: dict, out_dir: str, gpu: str) -> None:
         "// (half-)length 2^L, so that all of them compute a size with the same radices.",
         "// kTunedVariant[kind][L]: batched kernel variant for kind (0 complex forward,",
         "// 1 complex inverse, 2 real forward, 3 real inverse): 0 plain, 2 / 3 pipelined",
-        "// with 2 / 3 bulk-copy buffers, 6 / 7 CTAs of about 512 / 128 threads (the",
-        "// same arithmetic as plain).",
+        "// with 2 / 3 bulk-copy buffers, 6 / 7 CTAs of about 512 / 128 threads, 8",
+        "// pipelined with one buffer and a split exchange area (the same arithmetic",
+        "// as plain).",
         "#pragma once",
         "namespace ckg {",
         f"constexpr signed char kTunedLog2R[{len(LOG2_RANGE)}] = {{" + ", ".join(str(v) for v in lr) + "};",

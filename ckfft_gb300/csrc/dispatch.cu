@@ -111,7 +111,7 @@ int variant_for(Kind kind, int log2c)
         const char* v = std::getenv("CKFFT_CUDA_VARIANT");
         if (!v || !*v) return -1;
         const int x = std::atoi(v);
-        return (x == 0 || (x >= 2 && x <= 7)) ? x : -1;
+        return (x == 0 || (x >= 2 && x <= 8)) ? x : -1;
     }();
     if (forced >= 0) return forced;
     if (kind < 0 || kind > 3 || log2c < 0 || log2c > 14) return 0;

@@ -131,14 +131,16 @@ k_pipe(const float2* __restrict__ in, float2* __restrict__ out, long long ngroup
 }
 
 // ------------------------------------------------ split-exchange form
-// Complex frames too large for one buffer to be both the landing zone and
-// the exchange area twice over (2^14: 128 KiB a frame) keep the two apart:
-// one landing buffer the size of a group, and an exchange area that moves
-// the x parts, then the y parts, through a float image padded every 32
-// elements (68 KiB at 2^14; 196 KiB a CTA in all).  The copy of the next
-// group is issued as soon as every thread holds its inputs, so it lands
-// while this group's stages and stores run.  Same stages, twiddles and
-// positions as the other forms: the same results bit for bit.
+// The landing zone and the exchange area kept apart (kernel variant 8,
+// complex kinds): one landing buffer the size of a group, and an exchange
+// area that moves the x parts, then the y parts, through a float image
+// padded every 32 elements.  For frames too large for one buffer to be both
+// twice over (2^14: 128 KiB a frame, 68 KiB of exchange area, 196 KiB a
+// CTA), and for sizes where the smaller footprint lets two persistent CTAs
+// share an SM (2^13: 98 KiB).  The copy of the next group is issued as soon
+// as every thread holds its inputs, so it lands while this group's stages
+// and stores run.  Same stages, twiddles and positions as the other forms:
+// the same results bit for bit.
 template <int L, int KIND>
 struct PipeSxCfg {
     using C = SmallCfg<L>;
@@ -148,8 +150,10 @@ struct PipeSxCfg {
     static constexpr int XLEN = N + (N >> 5) + 1;                    // floats per frame image
     static constexpr int XBUF = (C::TPB * XLEN + 3) / 4 * 4;         // floats (16-byte multiple)
     static constexpr size_t SMEM = sizeof(float2) * (size_t)LAND + sizeof(float) * (size_t)XBUF;
-    static constexpr bool FITS = (KIND == C2C_FWD || KIND == C2C_INV) && !PipeCfg<L, KIND, 2>::FITS &&
-                                 SMEM <= 227 * 1024 && C::T % 32 == 0;
+    // 32 values per thread (stage spans 1, 32, 1024, ...: compile-time image
+    // offsets), complex kinds, one CTA's shared memory
+    static constexpr bool FITS = (KIND == C2C_FWD || KIND == C2C_INV) && SMEM <= 227 * 1024 && C::T % 32 == 0 &&
+                                 C::R == 32;
 };
 
 __device__ __forceinline__ int pad32(int pos) { return pos + (pos >> 5); }
@@ -300,13 +304,6 @@ cudaError_t attr_pipe()
 {
     using P = PipeCfg<L, KIND, NBUF>;
     if constexpr (!P::FITS) {
-        using X = PipeSxCfg<L, KIND>;
-        if constexpr (X::FITS) {
-            cudaError_t e = cudaFuncSetAttribute(k_pipe_sx<L, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)X::SMEM);
-            if (e != cudaSuccess) return e;
-            return cudaFuncSetAttribute(k_pipe_sx<L, KIND>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        }
         return cudaSuccess;
     } else {
         cudaError_t e = cudaFuncSetAttribute(k_pipe<L, KIND, NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM);
@@ -325,18 +322,6 @@ cudaError_t launch_pipe(const void* in, void* out, long long count, long long in
     using C = SmallCfg<L>;
     *done = 0;
     if constexpr (!P::FITS) {
-        // the split-exchange form, one landing buffer whatever NBUF asks
-        using X = PipeSxCfg<L, KIND>;
-        if constexpr (X::FITS) {
-            const long long ngroups = count / C::TPB;
-            if (ngroups < 1 || in_dist != X::N || ((uintptr_t)in & 15) || (X::GROUP_BYTES & 15) || !err)
-                return cudaSuccess;
-            const int grid = pipe_sx_grid<L, KIND>(ngroups);
-            const cudaError_t e = launch_pdl(k_pipe_sx<L, KIND>, dim3(grid), dim3(C::THREADS), X::SMEM, s,
-                                             (const float2*)in, (float2*)out, ngroups, out_dist, tw, err);
-            *done = ngroups * C::TPB;
-            return e;
-        }
         return cudaSuccess;
     } else {
         const long long ngroups = count / C::TPB;
@@ -344,6 +329,43 @@ cudaError_t launch_pipe(const void* in, void* out, long long count, long long in
             return cudaSuccess;
         const int grid = pipe_grid<L, KIND, NBUF>(ngroups);
         const cudaError_t e = launch_pdl(k_pipe<L, KIND, NBUF>, dim3(grid), dim3(C::THREADS), P::SMEM, s,
+                                         (const float2*)in, (float2*)out, ngroups, out_dist, tw, err);
+        *done = ngroups * C::TPB;
+        return e;
+    }
+}
+
+template <int L, int KIND>
+cudaError_t attr_pipe_sx()
+{
+    using X = PipeSxCfg<L, KIND>;
+    if constexpr (!X::FITS) {
+        return cudaSuccess;
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(k_pipe_sx<L, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)X::SMEM);
+        if (e != cudaSuccess) return e;
+        return cudaFuncSetAttribute(k_pipe_sx<L, KIND>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    }
+}
+
+// Runs the whole groups of a batch through k_pipe_sx (frames back to back,
+// 16-byte aligned); frames handled in *done (0 when the form does not apply).
+template <int L, int KIND>
+cudaError_t launch_pipe_sx(const void* in, void* out, long long count, long long in_dist, long long out_dist,
+                           const float2* tw, unsigned* err, cudaStream_t s, long long* done)
+{
+    using X = PipeSxCfg<L, KIND>;
+    using C = SmallCfg<L>;
+    *done = 0;
+    if constexpr (!X::FITS) {
+        return cudaSuccess;
+    } else {
+        const long long ngroups = count / C::TPB;
+        if (ngroups < 1 || in_dist != X::N || ((uintptr_t)in & 15) || (X::GROUP_BYTES & 15) || !err)
+            return cudaSuccess;
+        const int grid = pipe_sx_grid<L, KIND>(ngroups);
+        const cudaError_t e = launch_pdl(k_pipe_sx<L, KIND>, dim3(grid), dim3(C::THREADS), X::SMEM, s,
                                          (const float2*)in, (float2*)out, ngroups, out_dist, tw, err);
         *done = ngroups * C::TPB;
         return e;

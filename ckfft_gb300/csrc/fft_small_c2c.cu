@@ -22,6 +22,7 @@ static cudaError_t launch_c2c_any(const void* in, void* out, long long count, lo
         }
         if (nb == 2) e = launch_pipe<L, K, 2>(in, out, count, in_dist, out_dist, tw, device_error_word(), s, &done);
         else if (nb == 3) e = launch_pipe<L, K, 3>(in, out, count, in_dist, out_dist, tw, device_error_word(), s, &done);
+        else if (nb == 8) e = launch_pipe_sx<L, K>(in, out, count, in_dist, out_dist, tw, device_error_word(), s, &done);
         if (e != cudaSuccess) return e;
         if (done) count_launch();
     }
@@ -61,6 +62,8 @@ static cudaError_t attr_c2c_all()
         if (e == cudaSuccess) e = attr_pipe<L, C2C_INV, 2>();
         if (e == cudaSuccess) e = attr_pipe<L, C2C_FWD, 3>();
         if (e == cudaSuccess) e = attr_pipe<L, C2C_INV, 3>();
+        if (e == cudaSuccess) e = attr_pipe_sx<L, C2C_FWD>();
+        if (e == cudaSuccess) e = attr_pipe_sx<L, C2C_INV>();
     }
     return e;
 }

@@ -175,7 +175,8 @@ void set_last_error(const char* msg);
 constexpr int kPipeMinLog2 = 6;
 // Kernel variant for a single-CTA size: 0 plain (default shape), 2 / 3
 // pipelined with that many bulk-copy buffers, 4 / 5 half / twice the values
-// per thread, 6 / 7 CTAs of about 512 / 128 threads.  From the committed
+// per thread, 6 / 7 CTAs of about 512 / 128 threads, 8 pipelined with one
+// bulk-copy buffer and a separate split exchange area (complex kinds).  From the committed
 // autotune table (tuning_table.h) unless the CKFFT_CUDA_VARIANT environment
 // variable forces one variant (the autotuner uses it to measure each);
 // a variant that does not exist for a size runs the plain kernel.

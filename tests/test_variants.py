@@ -1,6 +1,6 @@
 """Every kernel variant the autotuner can choose for the single-CTA sizes
 (plain, pipelined with 2 / 3 buffers, half / twice the values per thread,
-512- / 128-thread CTAs), forced with CKFFT_CUDA_VARIANT in its own process,
+512- / 128-thread CTAs, pipelined with a split exchange area), forced with CKFFT_CUDA_VARIANT in its own process,
 against the oracle: complex 2^6 .. 2^14 and real 2^7 .. 2^15, forward and
 inverse, batches that end in a partial CTA."""
 import os
@@ -53,7 +53,7 @@ print("ok", worst)
 """
 
 
-@pytest.mark.parametrize("variant", [0, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [0, 2, 3, 4, 5, 6, 7, 8])
 def test_variant_matches_oracle(torch_cuda, variant):
     env = dict(os.environ, CKFFT_CUDA_VARIANT=str(variant))
     r = subprocess.run([sys.executable, "-c", f"ROOT = {ROOT!r}\n" + CHILD], env=env, capture_output=True,
