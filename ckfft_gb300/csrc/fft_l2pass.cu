@@ -16,7 +16,7 @@
 // intermediate bytes in DRAM).  At 2^17 it was slower (2779 vs 2857) and is
 // not used there.  Real transforms of 2^16 / 2^17 points (these half
 // lengths) run here too, the split fused into the row tiles and the merge
-// into the column tiles (pass_rows_split, pass_cols_merge): forward 2593 /
+// into the column tiles (pass_rows_split, pass_cols_merge): forward 2749 /
 // 2621 GB/s, inverse 2780 / 2656, against 2507 / 2609 and 2714 / 2554 for
 // the same fused passes through HBM.
 #include <cooperative_groups.h>
@@ -31,12 +31,14 @@ namespace ckg {
 
 constexpr int kL2Threads = 256;
 
-template <int LA, int LB>
+template <int LA, int LB, int KIND = 0>
 struct L2Cfg {
-    // CTAs per transform: 4 at 2^15, 8 at 2^16 (measured on GB300, batches
-    // of 1 GiB: 2^15 3663 GB/s with 4, 3513 with 8, 3474 with 2; 2^16 3591
-    // with 8, 3424 with 4, 3121 with 2)
-    static constexpr int K = LA + LB <= 15 ? 4 : 8;
+    // CTAs per transform: 4 at 2^15, 8 at 2^16 and for the real forward
+    // (measured on GB300, batches of 1 GiB: complex 2^15 3663 GB/s with 4,
+    // 3513 with 8, 3474 with 2; 2^16 3591 with 8, 3424 with 4, 3121 with 2;
+    // real n = 2^16 forward 2749 with 8, 2584 with 4, inverse 2777 with 4,
+    // 2689 with 8)
+    static constexpr int K = LA + LB <= 15 && KIND != 2 ? 4 : 8;
     using PA = PassCfg<LA, kL2Threads>;
     using PB = PassCfg<LB, kL2Threads>;
     static constexpr int SGA = kL2Threads / PA::THREADS;     // column tiles at once
@@ -71,11 +73,11 @@ __device__ __forceinline__ void cluster_barrier(cg::cluster_group& cluster)
 // fr != nullptr: transform f reads fr[f].in and writes fr[f].out (a grouped
 // launch of a job run) instead of in + f in_dist, out + f out_dist.
 template <int LA, int LB, int KIND>
-__global__ void __cluster_dims__(L2Cfg<LA, LB>::K, 1, 1) __launch_bounds__(kL2Threads, 4)
+__global__ void __cluster_dims__(L2Cfg<LA, LB, KIND>::K, 1, 1) __launch_bounds__(kL2Threads, 4)
 k_l2_c2c(const float2* __restrict__ in, float2* __restrict__ out, float2* __restrict__ scratch, long long in_dist,
          long long out_dist, const float2* __restrict__ tw, const FrameDesc* __restrict__ fr)
 {
-    using C = L2Cfg<LA, LB>;
+    using C = L2Cfg<LA, LB, KIND>;
     constexpr bool INV = KIND == 1 || KIND == 3;
     constexpr long long n = 1ll << (LA + LB);
     cg::cluster_group cluster = cg::this_cluster();
@@ -117,7 +119,7 @@ template <int LA, int LB, int KIND>
 static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, long long count, long long in_dist,
                                long long out_dist, const float2* tw, cudaStream_t s, const FrameDesc* fr = nullptr)
 {
-    using C = L2Cfg<LA, LB>;
+    using C = L2Cfg<LA, LB, KIND>;
     return launch_pdl(k_l2_c2c<LA, LB, KIND>, dim3((unsigned)(count * C::K)), dim3(kL2Threads), C::SMEM, s, in,
                       out, scratch, in_dist, out_dist, tw, fr);
 }

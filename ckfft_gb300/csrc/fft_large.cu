@@ -532,7 +532,7 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
 {
     // in: n floats per frame (n/2 packed complex), out: n/2+1 complex per frame
     // (half lengths 2^15 / 2^16: the cluster kernel with the split fused into
-    // its row tiles, 2593 / 2621 GB/s batched at n = 2^16 / 2^17 against 2507
+    // its row tiles, 2749 / 2621 GB/s batched at n = 2^16 / 2^17 against 2507
     // / 2609 for the fused two-pass form through HBM)
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
