@@ -13,8 +13,9 @@
 // Measured on GB300 (batches of 1 GiB): 2^15 3929 GB/s, 2^16 3851, against
 // 3145 / 3105 for the two-pass kernels through HBM; the kernel is bound by
 // the two passes' instructions, not by HBM (43 % DRAM throughput, no
-// intermediate bytes in DRAM).  At 2^17 it was slower (2779 vs 2857) and is
-// not used there.  Real transforms of 2^16 / 2^17 points (these half
+// intermediate bytes in DRAM).  At 2^17 (8-CTA clusters, 76 MB of
+// intermediate in flight) it ties with the two HBM passes (2935 / 2963
+// against 2928 / 2926 GB/s forward / inverse) and is not used there.  Real transforms of 2^16 / 2^17 points (these half
 // lengths) run here too, the split fused into the row tiles and the merge
 // into the column tiles (pass_rows_split, pass_cols_merge): forward 2749 /
 // 2621 GB/s, inverse 2780 / 2656, against 2507 / 2609 and 2714 / 2554 for
