@@ -563,10 +563,10 @@ def run_w1(args):
         yh = torch.empty_like(xh).pin_memory()
         ctx.check(ctx.batch("cfwd", n, frames, xh, Xh))
         t0 = time.perf_counter()
-        for _ in range(3):
+        for _ in range(args.steps):
             ctx.check(ctx.batch("cfwd", n, frames, xh, Xh))
             ctx.check(ctx.batch("cinv", n, frames, Xh, yh))
-        dt = (time.perf_counter() - t0) / 3
+        dt = (time.perf_counter() - t0) / args.steps
         line["e2e"] = {"value": round(2 * frames * per / dt / 1e9, 2), "unit": "GB/s",
                        "h2d_bytes_per_step": 2 * frames * n * 8, "d2h_bytes_per_step": 2 * frames * n * 8,
                        "ms_per_step": round(dt * 1e3, 3)}
