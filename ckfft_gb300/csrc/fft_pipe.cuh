@@ -131,8 +131,7 @@ k_pipe(const float2* __restrict__ in, float2* __restrict__ out, long long ngroup
 }
 
 // ------------------------------------------------ split-exchange form
-// The landing zone and the exchange area kept apart (kernel variant 8,
-// complex kinds): one landing buffer the size of a group, and an exchange
+// The landing zone and the exchange area kept apart (kernel variant 8): one landing buffer the size of a group, and an exchange
 // area that moves the x parts, then the y parts, through a float image
 // padded every 32 elements.  For frames too large for one buffer to be both
 // twice over (2^14: 128 KiB a frame, 68 KiB of exchange area, 196 KiB a
@@ -144,16 +143,20 @@ k_pipe(const float2* __restrict__ in, float2* __restrict__ out, long long ngroup
 template <int L, int KIND>
 struct PipeSxCfg {
     using C = SmallCfg<L>;
-    static constexpr int N = 1 << L;
-    static constexpr unsigned GROUP_BYTES = (unsigned)(C::TPB * N * sizeof(float2));
-    static constexpr int LAND = C::TPB * N;                          // float2
-    static constexpr int XLEN = N + (N >> 5) + 1;                    // floats per frame image
-    static constexpr int XBUF = (C::TPB * XLEN + 3) / 4 * 4;         // floats (16-byte multiple)
+    static constexpr int N = 1 << L;                                  // complex (half) length
+    static constexpr bool REAL = KIND == R2C || KIND == C2R;
+    // bytes of one bulk copy: the group's frames (complex, real forward), or
+    // for the real inverse the N bins from the first 16-byte aligned one
+    static constexpr unsigned COPY_BYTES = (unsigned)(C::TPB * N * sizeof(float2));
+    // landing slots; the real inverse's bins sit from slot 2 on, with one slot
+    // either side for the bin fetched by a plain load
+    static constexpr int LAND = KIND == C2R ? N + 4 : C::TPB * N;
+    static constexpr int XLEN = N + (N >> 5) + 1;                     // floats per frame image
+    static constexpr int XBUF = (C::TPB * XLEN + 3) / 4 * 4;          // floats (16-byte multiple)
     static constexpr size_t SMEM = sizeof(float2) * (size_t)LAND + sizeof(float) * (size_t)XBUF;
     // 32 values per thread (stage spans 1, 32, 1024, ...: compile-time image
-    // offsets), complex kinds, one CTA's shared memory
-    static constexpr bool FITS = (KIND == C2C_FWD || KIND == C2C_INV) && SMEM <= 227 * 1024 && C::T % 32 == 0 &&
-                                 C::R == 32;
+    // offsets), one CTA's shared memory; real kinds one frame per CTA
+    static constexpr bool FITS = SMEM <= 227 * 1024 && C::T % 32 == 0 && C::R == 32 && (!REAL || C::TPB == 1);
 };
 
 __device__ __forceinline__ int pad32(int pos) { return pos + (pos >> 5); }
@@ -205,15 +208,20 @@ __device__ __forceinline__ void stockham_split(float2 (&v)[1 << LOG2R], int t, c
     });
 }
 
+// in_dist / out_dist in float2 (real sides: packed pairs of reals).
+// C2C_FWD / C2C_INV: frames of N values back to back (in_dist = N), 16-byte
+// aligned.  R2C: N packed pairs in (in_dist = N, 16-byte aligned), N + 1 bins
+// out, the split through the float image.  C2R: N + 1 bins in (any in_dist),
+// N packed pairs out, the merge straight from the landing zone.
 template <int L, int KIND>
 __global__ void __launch_bounds__(SmallCfg<L>::THREADS, SmallCfg<L>::MINB)
-k_pipe_sx(const float2* __restrict__ in, float2* __restrict__ out, long long ngroups, long long out_dist,
-          const float2* __restrict__ tw, unsigned* err)
+k_pipe_sx(const float2* __restrict__ in, float2* __restrict__ out, long long ngroups, long long in_dist,
+          long long out_dist, const float2* __restrict__ tw, unsigned* err)
 {
     using P = PipeSxCfg<L, KIND>;
     using C = SmallCfg<L>;
     constexpr int N = P::N;
-    constexpr bool INV = KIND == C2C_INV;
+    constexpr bool INV = KIND == C2C_INV || KIND == C2R;
     extern __shared__ __align__(128) float2 smem[];
     __shared__ __align__(8) unsigned long long bar;
     float* xa = reinterpret_cast<float*>(smem + P::LAND);
@@ -225,21 +233,47 @@ k_pipe_sx(const float2* __restrict__ in, float2* __restrict__ out, long long ngr
         fence_mbar_init();
     }
     __syncthreads();
+    // real inverse: bin k of the frame at slot 2 + k - o, o = 1 when the
+    // frame's first bin is not 16-byte aligned (bins in pairs of 16 bytes)
+    auto odd = [&](long long grp) { return (int)(((uintptr_t)(in + grp * in_dist) >> 3) & 1); };
     auto issue = [&](long long grp) {
-        mbar_arrive_expect_tx(b, P::GROUP_BYTES);
-        bulk_load(smem_addr(smem), in + grp * (long long)P::LAND, P::GROUP_BYTES, b);
+        const float2* src = in + grp * in_dist;
+        mbar_arrive_expect_tx(b, P::COPY_BYTES);
+        if constexpr (KIND == C2R) {
+            // bins o .. o + N - 1 by bulk copy, the remaining one (N or 0) by
+            // a plain load outside the copied slots
+            const int o = odd(grp);
+            bulk_load(smem_addr(smem + 2), src + o, P::COPY_BYTES, b);
+            const int extra = o ? 0 : N;
+            smem[2 + extra - o] = src[extra];
+        } else {
+            bulk_load(smem_addr(smem), src, P::COPY_BYTES, b);
+        }
     };
     if (threadIdx.x == 0 && (long long)blockIdx.x < ngroups) issue(blockIdx.x);
+    if constexpr (KIND == C2R) __syncthreads();            // the first frame's plain-loaded bin
 
     long long failed_at = -1;
     for (long long i = 0;; ++i) {
         const long long grp = blockIdx.x + i * gridDim.x;
         if (grp >= ngroups) break;
         const bool ok = mbar_wait(b, (uint32_t)(i & 1), err);
-        const float2* land = smem + g * N;
         float2 v[C::R];
+        if constexpr (KIND == C2R) {
+            // the merge of c2r_load, operands from the landing zone
+            const float2* land = smem + 2 - odd(grp);
+            const float2* twn = tw + 2 * N;
+            const float2 w0 = __ldg(twn + t);
+            static_for<0, C::R>([&](auto mc) {
+                constexpr int m = decltype(mc)::value;
+                const int p = t + m * C::T;
+                v[m] = real_merge(land[p], land[N - p], split_twiddle<C::R, m, false>(w0, twn, p));
+            });
+        } else {
+            const float2* land = smem + g * N;
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) v[m] = land[t + m * C::T];
+            for (int m = 0; m < C::R; ++m) v[m] = land[t + m * C::T];
+        }
         // every input is in registers before the next copy overwrites the
         // landing zone; a timed-out wait anywhere stops the whole CTA
         if (__syncthreads_or(!ok)) { failed_at = i; break; }
@@ -250,10 +284,48 @@ k_pipe_sx(const float2* __restrict__ in, float2* __restrict__ out, long long ngr
                 issue(next);
             }
         }
-        stockham_split<L, C::LOG2R, INV, C::WARP>(v, t, tw, xa + g * P::XLEN);
-        float2* dst = out + (grp * C::TPB + g) * out_dist + t;
+        float* img = xa + g * P::XLEN;
+        stockham_split<L, C::LOG2R, INV, C::WARP>(v, t, tw, img);
+        if constexpr (KIND == R2C) {
+            // the split of split_store: partners Z[(N - k) mod N] through the
+            // float image, the x parts then the y parts
+            float zx[C::R / 2], zy[C::R / 2];
+            static_for<0, 2>([&](auto cc) {
+                constexpr int comp = decltype(cc)::value;
 #pragma unroll
-        for (int m = 0; m < C::R; ++m) __stcs(dst + m * C::T, v[m]);
+                for (int m = 0; m < C::R; ++m) img[pad32(t + m * C::T)] = comp ? v[m].y : v[m].x;
+                __syncthreads();
+#pragma unroll
+                for (int m = 0; m < C::R / 2; ++m) {
+                    const float f = img[pad32((N - t - m * C::T) & (N - 1))];
+                    if constexpr (comp) zy[m] = f;
+                    else zx[m] = f;
+                }
+                __syncthreads();
+            });
+            float2* dst = out + grp * out_dist;
+            const float2* twn = tw + 2 * N;
+            const float2 w0 = __ldg(twn + t);
+            static_for<0, C::R / 2>([&](auto mc) {
+                constexpr int m = decltype(mc)::value;
+                const int k = t + m * C::T;
+                const float2 z0 = v[m], z1 = make_float2(zx[m], zy[m]);
+                const float2 w = split_twiddle<C::R, m, false>(w0, twn, k);
+                const float sx = z0.x + z1.x, sy = z0.y - z1.y;
+                const float dx = z0.x - z1.x, dy = z0.y + z1.y;
+                const float px = fmaf(w.x, dx, -w.y * dy), py = fmaf(w.x, dy, w.y * dx);
+                __stcs(dst + k, make_float2(sx + py, sy - px));
+                __stcs(dst + (N - k), make_float2(sx - py, -(sy + px)));
+            });
+            if (t == 0) {
+                const float2 z = v[C::R / 2];                 // Z[N/2] = 2 conj of itself
+                __stcs(dst + N / 2, make_float2(z.x + z.x, -(z.y + z.y)));
+            }
+        } else {
+            float2* dst = out + (grp * C::TPB + g) * out_dist + t;
+#pragma unroll
+            for (int m = 0; m < C::R; ++m) __stcs(dst + m * C::T, v[m]);
+        }
     }
     if (failed_at >= 0 && threadIdx.x == 0) {
         // the copy of iteration failed_at may still be in flight: give it a
@@ -349,8 +421,10 @@ cudaError_t attr_pipe_sx()
     }
 }
 
-// Runs the whole groups of a batch through k_pipe_sx (frames back to back,
-// 16-byte aligned); frames handled in *done (0 when the form does not apply).
+// Runs the whole groups of a batch through k_pipe_sx; in_dist / out_dist in
+// float2 (packed pairs on the real sides).  Frames handled in *done (0 when
+// the form does not apply: complex and real forward inputs must be frames
+// back to back, 16-byte aligned; real inverse bins 8-byte aligned).
 template <int L, int KIND>
 cudaError_t launch_pipe_sx(const void* in, void* out, long long count, long long in_dist, long long out_dist,
                            const float2* tw, unsigned* err, cudaStream_t s, long long* done)
@@ -362,11 +436,12 @@ cudaError_t launch_pipe_sx(const void* in, void* out, long long count, long long
         return cudaSuccess;
     } else {
         const long long ngroups = count / C::TPB;
-        if (ngroups < 1 || in_dist != X::N || ((uintptr_t)in & 15) || (X::GROUP_BYTES & 15) || !err)
+        if (ngroups < 1 || !err || (X::COPY_BYTES & 15)) return cudaSuccess;
+        if (KIND == C2R ? (in_dist < X::N + 1 || ((uintptr_t)in & 7)) : (in_dist != X::N || ((uintptr_t)in & 15)))
             return cudaSuccess;
         const int grid = pipe_sx_grid<L, KIND>(ngroups);
         const cudaError_t e = launch_pdl(k_pipe_sx<L, KIND>, dim3(grid), dim3(C::THREADS), X::SMEM, s,
-                                         (const float2*)in, (float2*)out, ngroups, out_dist, tw, err);
+                                         (const float2*)in, (float2*)out, ngroups, in_dist, out_dist, tw, err);
         *done = ngroups * C::TPB;
         return e;
     }

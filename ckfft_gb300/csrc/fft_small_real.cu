@@ -23,6 +23,7 @@ static cudaError_t launch_real_any(const void* in, void* out, long long count, l
         }
         if (nb == 2) e = launch_pipe<LM, K, 2>(in, out, count, di, dout, tw, device_error_word(), s, &done);
         else if (nb == 3) e = launch_pipe<LM, K, 3>(in, out, count, di, dout, tw, device_error_word(), s, &done);
+        else if (nb == 8) e = launch_pipe_sx<LM, K>(in, out, count, di, dout, tw, device_error_word(), s, &done);
         if (e != cudaSuccess) return e;
         if (done) count_launch();
     }
@@ -64,6 +65,8 @@ static cudaError_t attr_real_all()
         if (e == cudaSuccess) e = attr_pipe<LM, C2R, 2>();
         if (e == cudaSuccess) e = attr_pipe<LM, R2C, 3>();
         if (e == cudaSuccess) e = attr_pipe<LM, C2R, 3>();
+        if (e == cudaSuccess) e = attr_pipe_sx<LM, R2C>();
+        if (e == cudaSuccess) e = attr_pipe_sx<LM, C2R>();
     }
     return e;
 }

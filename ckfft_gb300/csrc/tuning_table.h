@@ -12,9 +12,9 @@
 namespace ckg {
 constexpr signed char kTunedLog2R[15] = {0, 1, 2, 3, 4, 4, 3, 3, 4, 4, 4, 4, 4, 5, 5};
 constexpr signed char kTunedVariant[4][15] = {
-    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 7, 7, 0, 0, 8},   // cfwd
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 7, 7, 0, 8, 8},   // cfwd
     {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 7, 7, 0, 0, 8},   // cinv
-    {0, 0, 0, 0, 0, 0, 0, 7, 0, 7, 7, 7, 0, 0, 0},   // rfwd
-    {0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 2, 2, 0, 0, 0},   // rinv
+    {0, 0, 0, 0, 0, 0, 0, 7, 0, 7, 7, 7, 0, 0, 8},   // rfwd
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 2, 2, 0, 8, 8},   // rinv
 };
 }  // namespace ckg
