@@ -131,9 +131,9 @@ k_pipe(const float2* __restrict__ in, float2* __restrict__ out, long long ngroup
 }
 
 // ------------------------------------------------ split-exchange form
-// The landing zone and the exchange area kept apart (kernel variant 8): one landing buffer the size of a group, and an exchange
-// area that moves the x parts, then the y parts, through a float image
-// padded every 32 elements.  For frames too large for one buffer to be both
+// The landing zone and the exchange area kept apart (kernel variant 8): one
+// landing buffer the size of a group, and an exchange area that moves the x
+// parts, then the y parts, through a float image padded every 32 elements.  For frames too large for one buffer to be both
 // twice over (2^14: 128 KiB a frame, 68 KiB of exchange area, 196 KiB a
 // CTA), and for sizes where the smaller footprint lets two persistent CTAs
 // share an SM (2^13: 98 KiB).  The copy of the next group is issued as soon
@@ -205,6 +205,92 @@ __device__ __forceinline__ void stockham_split(float2 (&v)[1 << LOG2R], int t, c
         constexpr int st = decltype(sc)::value;
         stage_compute<LOG2N, LOG2R, S::lrs(st), S::lns(st), INV>(v, t, tw);
         if constexpr (st + 1 < S::nstages) exchange_split<LOG2N, LOG2R, S::lrs(st), S::lns(st), WARP>(v, t, xa);
+    });
+}
+
+// The real forward's last stage in the paired layout: thread t owns the
+// butterflies b_{2i} = t + i T and b_{2i+1} = NS - i T - t (NS / 2 for
+// t = i = 0) instead of t + u T.  Butterfly b's outputs sit at b + j NS and
+// those of NS - b at (NS - b) + (RS - 1 - j) NS = N - (b + j NS), so every
+// pair (k, N - k) of the split is in one thread's registers.  Each butterfly
+// is computed exactly as by stage_compute (its twiddles from k = b).
+template <int T, int NS>
+__device__ __forceinline__ int paired_butterfly(int t, int u)
+{
+    const int i = u >> 1;
+    if ((u & 1) == 0) return t + i * T;
+    return (t == 0 && i == 0) ? NS / 2 : NS - i * T - t;
+}
+
+template <int LOG2N, int LOG2R, bool WARP>
+__device__ __forceinline__ void stockham_split_paired(float2 (&v)[1 << LOG2R], int t, const float2* __restrict__ tw,
+                                                      float* xa)
+{
+    using S = Sched<LOG2N, LOG2R>;
+    constexpr int NST = S::nstages;
+    constexpr int R = 1 << LOG2R, T = (1 << LOG2N) / R;
+    constexpr int LRS = S::lrs(NST - 1), LNS = S::lns(NST - 1);
+    constexpr int RS = 1 << LRS, NS = 1 << LNS, U = R / RS;
+    static_assert(NST >= 2 && U % 2 == 0 && NS % 32 == 0 && NS == U * T, "paired last stage");
+    static_for<0, NST - 1>([&](auto sc) {
+        constexpr int st = decltype(sc)::value;
+        stage_compute<LOG2N, LOG2R, S::lrs(st), S::lns(st), false>(v, t, tw);
+        if constexpr (st + 2 < NST) {
+            exchange_split<LOG2N, LOG2R, S::lrs(st), S::lns(st), WARP>(v, t, xa);
+        } else {
+            // the last exchange: written as by exchange_split, read back in
+            // the paired layout, v[u + j U] = position b_u + j NS
+            constexpr int LRS0 = S::lrs(st), LNS0 = S::lns(st);
+            constexpr int RS0 = 1 << LRS0, NS0 = 1 << LNS0, U0 = R / RS0;
+            static_for<0, 2>([&](auto cc) {
+                constexpr int comp = decltype(cc)::value;
+#pragma unroll
+                for (int u = 0; u < U0; ++u) {
+                    const int b = t + u * T;
+                    const int base = ((b >> LNS0) << (LNS0 + LRS0)) + (b & (NS0 - 1));
+                    float* p = xa + pad32(base);
+#pragma unroll
+                    for (int j = 0; j < RS0; ++j) {
+                        const int off = NS0 == 1 ? j : j * (NS0 + NS0 / 32);
+                        p[off] = comp ? v[u + j * U0].y : v[u + j * U0].x;
+                    }
+                }
+                xsync<WARP>();
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const float* q = xa + pad32(paired_butterfly<T, NS>(t, u));
+#pragma unroll
+                    for (int j = 0; j < RS; ++j) {
+                        const float f = q[j * (NS + NS / 32)];
+                        if constexpr (comp) v[u + j * U].y = f;
+                        else v[u + j * U].x = f;
+                    }
+                }
+                xsync<WARP>();
+            });
+        }
+    });
+    // the last stage, butterfly by butterfly (stage_compute's arithmetic)
+    static_for<0, U>([&](auto uc) {
+        constexpr int u = decltype(uc)::value;
+        float2 x[RS];
+#pragma unroll
+        for (int j = 0; j < RS; ++j) x[j] = v[u + j * U];
+        const int k = paired_butterfly<T, NS>(t, u);
+        float2 w[RS];
+#pragma unroll
+        for (int p = 1; p < RS; p <<= 1) w[p] = tw_load<false>(tw + NS * RS / p, k);
+#pragma unroll
+        for (int j = 3; j < RS; ++j) {
+            if ((j & (j - 1)) == 0) continue;
+            const int hb = 1 << (31 - __clz(j));
+            w[j] = cmul(w[hb], w[j - hb]);
+        }
+#pragma unroll
+        for (int j = 1; j < RS; ++j) x[j] = cmul(x[j], w[j]);
+        dft<RS, false>(x);
+#pragma unroll
+        for (int j = 0; j < RS; ++j) v[u + j * U] = x[j];
     });
 }
 
@@ -285,43 +371,49 @@ k_pipe_sx(const float2* __restrict__ in, float2* __restrict__ out, long long ngr
             }
         }
         float* img = xa + g * P::XLEN;
-        stockham_split<L, C::LOG2R, INV, C::WARP>(v, t, tw, img);
         if constexpr (KIND == R2C) {
-            // the split of split_store: partners Z[(N - k) mod N] through the
-            // float image, the x parts then the y parts
-            float zx[C::R / 2], zy[C::R / 2];
-            static_for<0, 2>([&](auto cc) {
-                constexpr int comp = decltype(cc)::value;
-#pragma unroll
-                for (int m = 0; m < C::R; ++m) img[pad32(t + m * C::T)] = comp ? v[m].y : v[m].x;
-                __syncthreads();
-#pragma unroll
-                for (int m = 0; m < C::R / 2; ++m) {
-                    const float f = img[pad32((N - t - m * C::T) & (N - 1))];
-                    if constexpr (comp) zy[m] = f;
-                    else zx[m] = f;
-                }
-                __syncthreads();
-            });
+            // the last stage in the paired layout: both members of every
+            // split pair in this thread's registers; the split of split_store
+            // (same operands, twiddle W_2N^k of k = min(p, N - p)) from them
+            stockham_split_paired<L, C::LOG2R, C::WARP>(v, t, tw, img);
+            using S = Sched<L, C::LOG2R>;
+            constexpr int LRS = S::lrs(S::nstages - 1), LNS = S::lns(S::nstages - 1);
+            constexpr int RS = 1 << LRS, NS = 1 << LNS, U = C::R / RS;
             float2* dst = out + grp * out_dist;
             const float2* twn = tw + 2 * N;
-            const float2 w0 = __ldg(twn + t);
-            static_for<0, C::R / 2>([&](auto mc) {
-                constexpr int m = decltype(mc)::value;
-                const int k = t + m * C::T;
-                const float2 z0 = v[m], z1 = make_float2(zx[m], zy[m]);
-                const float2 w = split_twiddle<C::R, m, false>(w0, twn, k);
+            auto split_pair = [&](int k, float2 z0, float2 z1) {
+                const float2 w = tw_load<false>(twn, k);
                 const float sx = z0.x + z1.x, sy = z0.y - z1.y;
                 const float dx = z0.x - z1.x, dy = z0.y + z1.y;
                 const float px = fmaf(w.x, dx, -w.y * dy), py = fmaf(w.x, dy, w.y * dx);
                 __stcs(dst + k, make_float2(sx + py, sy - px));
                 __stcs(dst + (N - k), make_float2(sx - py, -(sy + px)));
+            };
+            static_for<0, U / 2>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                constexpr int u = 2 * i;
+                if (i == 0 && t == 0) {
+                    // butterflies 0 and NS / 2 pair with themselves
+#pragma unroll
+                    for (int j = 0; j < RS / 2; ++j) {
+                        split_pair(j * NS, v[u + j * U], v[u + ((RS - j) & (RS - 1)) * U]);
+                        split_pair(NS / 2 + j * NS, v[u + 1 + j * U], v[u + 1 + (RS - 1 - j) * U]);
+                    }
+                    const float2 z = v[u + (RS / 2) * U];          // X[N/2] = 2 conj Z[N/2]
+                    __stcs(dst + N / 2, make_float2(z.x + z.x, -(z.y + z.y)));
+                } else {
+                    const int b = paired_butterfly<C::T, NS>(t, u);
+#pragma unroll
+                    for (int j = 0; j < RS; ++j) {
+                        const int p = b + j * NS;
+                        const float2 zp = v[u + j * U], zq = v[u + 1 + (RS - 1 - j) * U];
+                        if (p < N - p) split_pair(p, zp, zq);
+                        else split_pair(N - p, zq, zp);
+                    }
+                }
             });
-            if (t == 0) {
-                const float2 z = v[C::R / 2];                 // Z[N/2] = 2 conj of itself
-                __stcs(dst + N / 2, make_float2(z.x + z.x, -(z.y + z.y)));
-            }
         } else {
+            stockham_split<L, C::LOG2R, INV, C::WARP>(v, t, tw, img);
             float2* dst = out + (grp * C::TPB + g) * out_dist + t;
 #pragma unroll
             for (int m = 0; m < C::R; ++m) __stcs(dst + m * C::T, v[m]);
