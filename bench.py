@@ -69,10 +69,10 @@ def parse_args():
     ap.add_argument("--no-w5", action="store_true", help="default line: leave out the serving sub-object")
     ap.add_argument("--requests", type=int, default=10000, help="w5: requests per offered load")
     ap.add_argument("--direct-mb", type=int, default=8, help="w5: requests this large skip batching")
-    ap.add_argument("--workload", choices=["w1", "w2", "w3", "w4", "w5", "sizes"], default="w2",
+    ap.add_argument("--workload", choices=["w1", "w2", "w3", "w4", "w5", "sizes", "layouts"], default="w2",
                     help="w2 (default): real n=4096 x 65536 frames; w1: complex n=1024 x 4096 round trip; "
                          "w3: large single complex transforms; w4: uneven mixed batch; w5: serving; "
-                         "sizes: batched GB/s per size and kind")
+                         "sizes: batched GB/s per size and kind; layouts: distance-1 advanced layouts")
     ap.add_argument("--sizes", default=",".join(str(i) for i in range(25)),
                     help="sizes workload: comma-separated log2 n")
     ap.add_argument("--kinds", default="cfwd,cinv,rfwd,rinv", help="sizes workload: comma-separated kinds")
@@ -572,6 +572,78 @@ def run_w1(args):
                        "ms_per_step": round(dt * 1e3, 3)}
     if not args.no_cpu:
         line["cpu_baseline"] = time_cpu_complex(n, frames)
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+# (name, kind, n, transforms, distance-1 side: "both" / "in" / "out")
+LAYOUT_CASES = [
+    ("interleaved channels, complex n=4096 x 16384, both sides", "cfwd", 4096, 16384, "both"),
+    ("interleaved channels, complex n=4096 x 16384, input side", "cfwd", 4096, 16384, "in"),
+    ("interleaved reals -> spectra, n=4096 x 16384", "rfwd", 4096, 16384, "in"),
+    ("spectra -> interleaved reals, n=4096 x 16384", "rinv", 4096, 16384, "out"),
+    ("matrix columns, complex 1024 x 65536", "cfwd", 1024, 65536, "both"),
+    ("interleaved channels, complex n=2^16 x 1024, both sides", "cfwd", 1 << 16, 1024, "both"),
+]
+
+
+def run_layouts(args):
+    """Distance-1 advanced layouts through CkFftCuda*Strided (device buffers,
+    CUDA events on the launching stream) against the contiguous batch of the
+    same work; GB/s of algorithmic bytes (each element read or written once)."""
+    import torch
+    from ckfft_gb300 import binding
+    from ckfft_gb300.workloads import algorithmic_bytes
+
+    ctx = binding.Context(max(c[2] for c in LAYOUT_CASES))
+    stream = torch.cuda.Stream()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(11)
+    steps = max(3, min(args.steps, 20))
+    table = {}
+
+    def timed(call):
+        for _ in range(3):
+            ctx.check(call())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(steps):
+            call()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / steps
+
+    for name, kind, n, count, side in LAYOUT_CASES:
+        real = kind in ("rfwd", "rinv")
+        nin = n if kind != "rinv" else n // 2 + 1
+        nout = n if kind != "rfwd" else n // 2 + 1
+        tin = torch.float32 if kind == "rfwd" else torch.complex64
+        tout = torch.float32 if kind == "rinv" else torch.complex64
+        mk = (lambda rows, cols, dt: torch.randn((rows, cols), generator=g, device="cuda", dtype=dt))
+        din, dout = side in ("both", "in"), side in ("both", "out")
+        x = mk(nin, count, tin) if din else mk(count, nin, tin)
+        y = torch.empty((nout, count) if dout else (count, nout), device="cuda", dtype=tout)
+        isd = (count, 1) if din else (1, nin)
+        osd = (count, 1) if dout else (1, nout)
+        t_lay = timed(lambda: ctx.strided(kind, n, count, x, isd[0], isd[1], y, osd[0], osd[1], stream))
+        xc = torch.empty((count, nin), device="cuda", dtype=tin)
+        yc = torch.empty((count, nout), device="cuda", dtype=tout)
+        t_con = timed(lambda: ctx.batch(kind, n, count, xc, yc, stream))
+        per = count * algorithmic_bytes(real, n)
+        table[name] = {"gbs": round(per / t_lay / 1e9, 1), "contiguous_gbs": round(per / t_con / 1e9, 1),
+                       "ms": round(t_lay * 1e3, 4)}
+        del x, y, xc, yc
+    first = table[LAYOUT_CASES[0][0]]
+    peak, src = measured_peaks()
+    line = base_line(args, "advanced-layout batch GB/s (" + LAYOUT_CASES[0][0] + ")", first["gbs"], "GB/s",
+                     first["ms"] / 1e3 * args.steps,
+                     {"workload": "distance-1 layouts through CkFftCuda*Strided, device buffers",
+                      "l2": "every case larger than L2", "steps": steps})
+    line["table"] = table
+    line["roofline"] = {"bound": "hbm", "kernel": "transposes + contiguous batched kernels", "achieved": first["gbs"],
+                        "peak": peak, "unit": "GB/s", "frac": round(first["gbs"] / peak, 4), "peak_source": src,
+                        "traffic": None}
     print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -1113,7 +1185,8 @@ def main():
                          f"`python -m torch.distributed.run --nproc-per-node {args.gpus} bench.py --gpus {args.gpus}`\n")
         raise SystemExit(2)
     if args.workload != "w2" and args.impl == "ours":
-        {"w1": run_w1, "w3": run_w3, "w4": run_w4, "w5": run_w5, "sizes": run_sizes}[args.workload](args)
+        {"w1": run_w1, "w3": run_w3, "w4": run_w4, "w5": run_w5, "sizes": run_sizes,
+         "layouts": run_layouts}[args.workload](args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -82,6 +82,41 @@ __global__ void k_scatter(const E* __restrict__ src, E* __restrict__ dst, long l
     }
 }
 
+// dst[c dp + r] = src[r sp + c] for r < rows, c < cols: 32 x 32 tiles through
+// shared memory, so both sides move runs of 32 consecutive elements (128 or
+// 256 bytes), and neighbouring CTAs take neighbouring tiles of the same rows.
+// SS / SD: evict-first loads / stores for the side read or written once.
+template <class E, bool SS, bool SD>
+__global__ void __launch_bounds__(256) k_transpose(const E* __restrict__ src, long long sp, E* __restrict__ dst,
+                                                   long long dp, long long rows, long long cols)
+{
+    __shared__ E tile[32][33];
+    const long long tiles_c = (cols + 31) / 32, tiles = tiles_c * ((rows + 31) / 32);
+    const int x = threadIdx.x & 31, y = threadIdx.x >> 5;
+    for (long long b = blockIdx.x; b < tiles; b += gridDim.x) {
+        const long long r0 = (b / tiles_c) * 32, c0 = (b % tiles_c) * 32;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const long long r = r0 + y + 8 * k, c = c0 + x;
+            if (r < rows && c < cols) {
+                const E* q = src + r * sp + c;
+                tile[y + 8 * k][x] = SS ? __ldcs(q) : *q;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const long long c = c0 + y + 8 * k, r = r0 + x;
+            if (r < rows && c < cols) {
+                E* q = dst + c * dp + r;
+                if constexpr (SD) __stcs(q, tile[x][y + 8 * k]);
+                else *q = tile[x][y + 8 * k];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------- launch
 
 template <class C>
@@ -179,6 +214,33 @@ cudaError_t launch_gather(const void* src, long long stride, long long dist, voi
     else return cudaErrorInvalidValue;
     count_launch();
     return cudaGetLastError();
+}
+
+template <class E>
+static cudaError_t launch_transpose_e(const void* src, long long sp, void* dst, long long dp, long long rows,
+                                      long long cols, bool stream_src, bool stream_dst, cudaStream_t s)
+{
+    const long long tiles = ((rows + 31) / 32) * ((cols + 31) / 32);
+    const unsigned grid = (unsigned)(tiles < 152 * 8 ? tiles : 152 * 8);
+    const E* a = (const E*)src;
+    E* b = (E*)dst;
+    if (stream_src && stream_dst) k_transpose<E, true, true><<<grid, 256, 0, s>>>(a, sp, b, dp, rows, cols);
+    else if (stream_src) k_transpose<E, true, false><<<grid, 256, 0, s>>>(a, sp, b, dp, rows, cols);
+    else if (stream_dst) k_transpose<E, false, true><<<grid, 256, 0, s>>>(a, sp, b, dp, rows, cols);
+    else k_transpose<E, false, false><<<grid, 256, 0, s>>>(a, sp, b, dp, rows, cols);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transpose(const void* src, long long sp, void* dst, long long dp, long long rows, long long cols,
+                             int esize, bool stream_src, bool stream_dst, cudaStream_t s)
+{
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    cudaError_t e;
+    if (esize == 8) e = launch_transpose_e<float2>(src, sp, dst, dp, rows, cols, stream_src, stream_dst, s);
+    else if (esize == 4) e = launch_transpose_e<float>(src, sp, dst, dp, rows, cols, stream_src, stream_dst, s);
+    else return cudaErrorInvalidValue;
+    if (e == cudaSuccess) count_launch();
+    return e;
 }
 
 cudaError_t launch_scatter(const void* src, void* dst, long long stride, long long dist, long long count,

@@ -52,6 +52,11 @@ cudaError_t launch_gather(const void* src, long long stride, long long dist, voi
                           long long len, int esize, cudaStream_t stream);
 cudaError_t launch_scatter(const void* src, void* dst, long long stride, long long dist, long long count,
                            long long len, int esize, cudaStream_t stream);
+// dst[c dp + r] = src[r sp + c] for r < rows, c < cols, elements of esize 4
+// or 8 bytes (pitches in elements); stream_src / stream_dst: evict-first
+// loads / stores for a side touched once.
+cudaError_t launch_transpose(const void* src, long long sp, void* dst, long long dp, long long rows, long long cols,
+                             int esize, bool stream_src, bool stream_dst, cudaStream_t stream);
 
 // Fused steps around the real transforms (single-CTA sizes, 8 <= n <= 2^15):
 // windowed frames at a hop -> real forward -> bins x scale; bins x filter x

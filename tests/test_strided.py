@@ -90,6 +90,12 @@ LAYOUTS = [
     ("inter-real-128-in", "rfwd", 128, 70, 70, 1, 2, 130),
     ("inter-real-128-out", "rinv", 128, 65, 1, 65, 65, 1),
     ("inter-real-4096-in-out-strided", "rfwd", 4096, 9, 9, 1, 9, 1),
+    # distance 1 beyond the distance-1 kernels: transposed chunks through
+    # contiguous rows (50 transforms of 2^16: chunks of 32 and 18)
+    ("transposed-2^16-both-two-chunks", "cfwd", 1 << 16, 50, 50, 1, 51, 1),
+    ("transposed-2^14-in", "cinv", 1 << 14, 40, 41, 1, 1, 1 << 14),
+    ("transposed-real-2^16-out", "rinv", 1 << 16, 33, 1, (1 << 15) + 1, 33, 1),
+    ("transposed-real-2^18-in", "rfwd", 1 << 18, 3, 3, 1, 1, (1 << 17) + 1),
 ]
 
 
