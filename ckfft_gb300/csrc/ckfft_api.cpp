@@ -592,17 +592,23 @@ int check_call(const CkFftContext* c, bool inverse, int n, const void* in, const
 // ------------------------------------------------------------ strided batches
 
 // Distance-1 layouts (interleaved channels, matrix columns) of the sizes the
-// distance-1 kernels of fft_inter.cu do not cover run as chunks of F
+// distance-1 kernels of fft_inter.cu do not cover, and complex transforms
+// from 2^12 whose input side alone is distance-1, run as chunks of F
 // transforms: each distance-1 side is transposed between the layout and
-// contiguous rows of a scratch block sized to stay in L2 (48 MiB), and the
+// contiguous rows of a scratch block sized to stay in L2 (96 MiB), and the
 // contiguous batched kernels transform the rows.  The transposes move runs
 // of 32 transforms (128 / 256 contiguous bytes of every layout row), and the
 // transforms are the contiguous path's own, bit for bit.  A side that is not
 // distance-1 must be contiguous rows (stride 1) the batched kernels read
-// directly.  Measured on GB300: complex n = 2^16 x 1024 interleaved on both
-// sides 1172 GB/s against 542 through the element-wise gather / scatter;
-// where the distance-1 kernels apply they stay ahead (n = 4096 x 16384 both
-// sides 2253 against 1728, matrix columns 1024 x 65536 3237 against 1848).
+// directly.  Measured on GB300 (GB/s): complex n = 2^16 x 1024 on both
+// sides 1555 against 542 through the element-wise gather / scatter; n = 4096
+// x 16384 with the input side alone distance-1 3092 against 2693 for the
+// distance-1 kernel; where that kernel covers both sides or a real side it
+// stays ahead (n = 4096 both sides 2253 against 2071, reals in 2723 against
+// 2566, reals out 3128 against 2280, matrix columns 1024 x 65536 3222
+// against 2218).
+
+constexpr size_t kTransposeChunkBytes = 96ull << 20;
 
 cudaError_t enqueue_transposed(CkFftContext* c, const Work& w, const void* in, long long is, void* out,
                                long long os, bool cin, bool cout, cudaStream_t s)
@@ -610,7 +616,7 @@ cudaError_t enqueue_transposed(CkFftContext* c, const Work& w, const void* in, l
     const int ein = w.kind == ckg::R2C ? 4 : 8, eout = w.kind == ckg::C2R ? 4 : 8;
     const long long ni = (long long)(w.in_bytes / ein), no = (long long)(w.out_bytes / eout);
     const size_t per = (cin ? w.in_bytes : 0) + (cout ? w.out_bytes : 0);
-    long long F = (long long)((48ull << 20) / per);
+    long long F = (long long)((kTransposeChunkBytes) / per);
     if (F >= 32) F = F / 32 * 32;                     // whole transpose tiles
     if (F < 1) F = 1;
     if (F > w.count) F = w.count;
@@ -659,7 +665,8 @@ cudaError_t enqueue_strided(CkFftContext* c, const Work& w, const void* in, long
     }
     // consecutive transforms adjacent (interleaved channels, matrix columns)
     const bool cin = w.in_dist == 1 && is > 1, cout = w.out_dist == 1 && os > 1;
-    if (ckg::inter_applies(w.kind, w.log2n, cin, cout))
+    const bool complex_in_only = !is_real(w.kind) && cin && !cout && w.log2n >= 12;
+    if (!complex_in_only && ckg::inter_applies(w.kind, w.log2n, cin, cout))
         return ckg::launch_inter(w.kind, w.log2n, in, out, w.count, ckg::Layout{is, w.in_dist, os, w.out_dist}, cin,
                                  cout, c->dtw, s);
     if ((cin || cout) && (cin || in_rows) && (cout || out_rows))

@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(256) k_transpose(const E* __restrict__ src, lo
     __shared__ E tile[32][33];
     const long long tiles_c = (cols + 31) / 32, tiles = tiles_c * ((rows + 31) / 32);
     const int x = threadIdx.x & 31, y = threadIdx.x >> 5;
+    pdl_start();
     for (long long b = blockIdx.x; b < tiles; b += gridDim.x) {
         const long long r0 = (b / tiles_c) * 32, c0 = (b % tiles_c) * 32;
 #pragma unroll
@@ -224,11 +225,10 @@ static cudaError_t launch_transpose_e(const void* src, long long sp, void* dst, 
     const unsigned grid = (unsigned)(tiles < 152 * 8 ? tiles : 152 * 8);
     const E* a = (const E*)src;
     E* b = (E*)dst;
-    if (stream_src && stream_dst) k_transpose<E, true, true><<<grid, 256, 0, s>>>(a, sp, b, dp, rows, cols);
-    else if (stream_src) k_transpose<E, true, false><<<grid, 256, 0, s>>>(a, sp, b, dp, rows, cols);
-    else if (stream_dst) k_transpose<E, false, true><<<grid, 256, 0, s>>>(a, sp, b, dp, rows, cols);
-    else k_transpose<E, false, false><<<grid, 256, 0, s>>>(a, sp, b, dp, rows, cols);
-    return cudaGetLastError();
+    if (stream_src && stream_dst) return launch_pdl(k_transpose<E, true, true>, dim3(grid), dim3(256), 0, s, a, sp, b, dp, rows, cols);
+    if (stream_src) return launch_pdl(k_transpose<E, true, false>, dim3(grid), dim3(256), 0, s, a, sp, b, dp, rows, cols);
+    if (stream_dst) return launch_pdl(k_transpose<E, false, true>, dim3(grid), dim3(256), 0, s, a, sp, b, dp, rows, cols);
+    return launch_pdl(k_transpose<E, false, false>, dim3(grid), dim3(256), 0, s, a, sp, b, dp, rows, cols);
 }
 
 cudaError_t launch_transpose(const void* src, long long sp, void* dst, long long dp, long long rows, long long cols,
