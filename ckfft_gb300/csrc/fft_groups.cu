@@ -5,8 +5,7 @@
 // kernel.  The frame bodies are the batched kernels' (fft_small.cuh); the
 // 2^15 / 2^16 complex groups and the real 2^16 / 2^17 groups use the
 // cluster two-pass kernel with its table argument (fft_l2pass.cu; real: the
-// split / merge fused into its tiles).  The fused two-pass table kernels of
-// fft_large.cu stay for a build that takes the real kinds off that kernel.
+// split / merge fused into its tiles).
 #include "fft_small.cuh"
 #include "jobs.h"
 #include "kernels.h"
@@ -106,15 +105,12 @@ cudaError_t launch_group(int op, int log2a, const FrameDesc* fr, long long count
                          void* scratch, size_t scratch_bytes, cudaStream_t s)
 {
     if (count <= 0) return cudaSuccess;
-    if (log2a > 14 && op == U_R2C && l2pass_supported(log2a) && l2pass_real(2))
-        return launch_l2pass_table(2, log2a, fr, count, tw, scratch, scratch_bytes, s);
-    if (log2a > 14 && op == U_C2R && l2pass_supported(log2a) && l2pass_real(3))
-        return launch_l2pass_table(3, log2a, fr, count, tw, scratch, scratch_bytes, s);
-    if (log2a > 14 && op == U_R2C) return launch_r2c_table(log2a, fr, count, tw, scratch, scratch_bytes, s);
-    if (log2a > 14 && op == U_C2R) return launch_c2r_table(log2a, fr, count, tw, scratch, scratch_bytes, s);
     if (log2a > 14) {
-        if (op != U_C2C_FWD && op != U_C2C_INV) return cudaErrorInvalidValue;
-        return launch_l2pass_table(op == U_C2C_INV ? 1 : 0, log2a, fr, count, tw, scratch, scratch_bytes, s);
+        // the cluster two-pass kernel: complex, or real with the split / merge
+        // fused into its tiles (kind 2 / 3)
+        const int kind = op == U_C2C_FWD ? 0 : op == U_C2C_INV ? 1 : op == U_R2C ? 2 : op == U_C2R ? 3 : -1;
+        if (kind < 0) return cudaErrorInvalidValue;
+        return launch_l2pass_table(kind, log2a, fr, count, tw, scratch, scratch_bytes, s);
     }
     cudaError_t e;
     switch (op) {

@@ -127,11 +127,6 @@ static cudaError_t launch_l2_L(const float2* in, float2* out, float2* scratch, l
 
 bool l2pass_supported(int log2n) { return log2n >= 15 && log2n <= 16; }
 
-// Real kinds on this kernel (bit 0: forward, bit 1: inverse).
-constexpr int kL2Real = 3;
-
-bool l2pass_real(int kind) { return (kind == 2 && (kL2Real & 1)) || (kind == 3 && (kL2Real & 2)); }
-
 // kind: 0 / 1 complex forward / inverse, 2 / 3 real forward / inverse of
 // 2^(log2n+1) reals (log2n: the complex half length); dists in complex units.
 cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,

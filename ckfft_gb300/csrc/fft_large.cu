@@ -131,64 +131,6 @@ k_cols_merge(const float2* __restrict__ in, float2* __restrict__ out, int log2n2
                                                                     blockIdx.x % tiles, threadIdx.x, smem, tw);
 }
 
-// The same two passes over a table of transforms (a grouped launch of a job
-// run): transform f reads fr[f].in and writes fr[f].out, its intermediate at
-// tmp + f M.
-template <int LA>
-__global__ void __launch_bounds__(BPass<LA>::THREADS, ColsMinBlocks<LA>::value)
-k_cols_table(const FrameDesc* __restrict__ fr, float2* __restrict__ tmp, int log2n2, const float2* __restrict__ tw)
-{
-    using P = BPass<LA>;
-    extern __shared__ float2 smem[];
-    pdl_start();
-    const long long tiles = (1ll << log2n2) / P::C;
-    const long long f = blockIdx.x / tiles;
-    pass_cols<LA, false, false, BatchMaxT<LA>::value, BatchCMax<LA>::value>(
-        fr[f].in, tmp + (f << (LA + log2n2)), log2n2, blockIdx.x % tiles, threadIdx.x, smem, tw);
-}
-
-template <int LB>
-__global__ void __launch_bounds__(BPass<LB>::THREADS)
-k_rows_split_table(const float2* __restrict__ tmp, const FrameDesc* __restrict__ fr, int log2n1,
-                   const float2* __restrict__ tw)
-{
-    using P = BPass<LB>;
-    extern __shared__ float2 smem[];
-    pdl_start();
-    const long long tiles = (1ll << log2n1) / P::C;
-    const long long f = blockIdx.x / tiles;
-    pass_rows_split<LB, BatchMaxT<LB>::value>(tmp + (f << (log2n1 + LB)), fr[f].out, log2n1, blockIdx.x % tiles,
-                                              threadIdx.x, smem, tw, log2n1);
-}
-
-template <int LA>
-__global__ void __launch_bounds__(BPass<LA>::THREADS, ColsMinBlocks<LA>::value)
-k_cols_merge_table(const FrameDesc* __restrict__ fr, float2* __restrict__ tmp, int log2n2,
-                   const float2* __restrict__ tw)
-{
-    using P = BPass<LA>;
-    extern __shared__ float2 smem[];
-    pdl_start();
-    const long long tiles = (1ll << log2n2) / P::C;
-    const long long f = blockIdx.x / tiles;
-    pass_cols_merge<LA, BatchMaxT<LA>::value, BatchCMax<LA>::value>(
-        fr[f].in, tmp + (f << (LA + log2n2)), log2n2, blockIdx.x % tiles, threadIdx.x, smem, tw);
-}
-
-template <int LB>
-__global__ void __launch_bounds__(BPass<LB>::THREADS)
-k_rows_inv_table(const float2* __restrict__ tmp, const FrameDesc* __restrict__ fr, int log2n1,
-                 const float2* __restrict__ tw)
-{
-    using P = BPass<LB>;
-    extern __shared__ float2 smem[];
-    pdl_start();
-    const long long tiles = (1ll << log2n1) / P::C;
-    const long long f = blockIdx.x / tiles;
-    pass_rows_xt<LB, true, false, BatchMaxT<LB>::value, true, BatchCMax<LB>::value>(
-        tmp + (f << (log2n1 + LB)), fr[f].out, log2n1, blockIdx.x % tiles, threadIdx.x, smem, tw);
-}
-
 // --------------------------- real split / merge as passes of their own
 // (used only when the scratch array is not 128-byte aligned)
 
@@ -457,75 +399,6 @@ static cudaError_t launch_r2c_rows_split(int lm, const float2* in, float2* out, 
     return cudaSuccess;
 }
 
-// Real forward of a table of transforms of 2^(lm+1) reals (half lengths
-// 2^15, 2^16: columns 2^7 / 2^8 long, rows 2^8), the split fused into the
-// row pass; scratch holds the intermediates of one launch group.
-cudaError_t launch_r2c_table(int lm, const FrameDesc* fr, long long count, const float2* tw, void* scratch,
-                             size_t scratch_bytes, cudaStream_t s)
-{
-    const LargePlan p = large_plan(lm);
-    if (lm < 15 || lm > 16 || p.log2n2 != 8) return cudaErrorInvalidValue;
-    if (count <= 0) return cudaSuccess;
-    const long long M = 1ll << lm;
-    const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)M));
-    if (group < 1 || ((uintptr_t)scratch & 127)) return cudaErrorInvalidValue;
-    float2* tmp = (float2*)scratch;
-    using B = BPass<8>;
-    for (long long off = 0; off < count; off += group) {
-        const long long cnt = count - off < group ? count - off : group;
-        cudaError_t e;
-        if (p.log2n1 == 7) {
-            using A = BPass<7>;
-            e = launch_pdl(k_cols_table<7>, dim3((unsigned)(cnt * ((1ll << 8) / A::C))), dim3(A::THREADS), A::SMEM, s,
-                           fr + off, tmp, 8, tw);
-        } else {
-            using A = BPass<8>;
-            e = launch_pdl(k_cols_table<8>, dim3((unsigned)(cnt * ((1ll << 8) / A::C))), dim3(A::THREADS), A::SMEM, s,
-                           fr + off, tmp, 8, tw);
-        }
-        if (e == cudaSuccess)
-            e = launch_pdl(k_rows_split_table<8>, dim3((unsigned)(cnt * ((1ll << p.log2n1) / B::C))), dim3(B::THREADS),
-                           B::SMEM, s, (const float2*)tmp, fr + off, p.log2n1, tw);
-        if (e != cudaSuccess) return e;
-        count_launch(2);
-    }
-    return cudaSuccess;
-}
-
-// Real inverse of a table of transforms to 2^(lm+1) reals (half lengths
-// 2^15, 2^16), the merge fused into the column pass.
-cudaError_t launch_c2r_table(int lm, const FrameDesc* fr, long long count, const float2* tw, void* scratch,
-                             size_t scratch_bytes, cudaStream_t s)
-{
-    const LargePlan p = large_plan(lm);
-    if (lm < 15 || lm > 16 || p.log2n2 != 8) return cudaErrorInvalidValue;
-    if (count <= 0) return cudaSuccess;
-    const long long M = 1ll << lm;
-    const long long group = (long long)(scratch_bytes / (sizeof(float2) * (size_t)M));
-    if (group < 1 || ((uintptr_t)scratch & 127)) return cudaErrorInvalidValue;
-    float2* tmp = (float2*)scratch;
-    using B = BPass<8>;
-    for (long long off = 0; off < count; off += group) {
-        const long long cnt = count - off < group ? count - off : group;
-        cudaError_t e;
-        if (p.log2n1 == 7) {
-            using A = BPass<7>;
-            e = launch_pdl(k_cols_merge_table<7>, dim3((unsigned)(cnt * ((1ll << 8) / A::C))), dim3(A::THREADS),
-                           A::SMEM, s, fr + off, tmp, 8, tw);
-        } else {
-            using A = BPass<8>;
-            e = launch_pdl(k_cols_merge_table<8>, dim3((unsigned)(cnt * ((1ll << 8) / A::C))), dim3(A::THREADS),
-                           A::SMEM, s, fr + off, tmp, 8, tw);
-        }
-        if (e == cudaSuccess)
-            e = launch_pdl(k_rows_inv_table<8>, dim3((unsigned)(cnt * ((1ll << p.log2n1) / B::C))), dim3(B::THREADS),
-                           B::SMEM, s, (const float2*)tmp, fr + off, p.log2n1, tw);
-        if (e != cudaSuccess) return e;
-        count_launch(2);
-    }
-    return cudaSuccess;
-}
-
 cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long count,
                              long long in_dist, long long out_dist, const float2* tw,
                              void* scratch, size_t scratch_bytes, cudaStream_t s)
@@ -537,7 +410,7 @@ cudaError_t launch_large_r2c(int log2n, const void* in, void* out, long long cou
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
     if (count <= 0) return cudaSuccess;
-    if (l2pass_supported(lm) && l2pass_real(2) && ((uintptr_t)scratch & 127) == 0)
+    if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_l2pass(2, lm, in, out, count, in_dist / 2, out_dist, tw, scratch, scratch_bytes, s);
     if (rows_split_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_r2c_rows_split(lm, (const float2*)in, (float2*)out, count, in_dist / 2, out_dist, tw,
@@ -622,7 +495,7 @@ cudaError_t launch_large_c2r(int log2n, const void* in, void* out, long long cou
     const int lm = log2n - 1;
     const long long M = 1ll << lm;
     if (count <= 0) return cudaSuccess;
-    if (l2pass_supported(lm) && l2pass_real(3) && ((uintptr_t)scratch & 127) == 0)
+    if (l2pass_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_l2pass(3, lm, in, out, count, in_dist, out_dist / 2, tw, scratch, scratch_bytes, s);
     if (cols_merge_supported(lm) && ((uintptr_t)scratch & 127) == 0)
         return launch_c2r_cols_merge(lm, (const float2*)in, (float2*)out, count, in_dist, out_dist / 2, tw,
@@ -653,14 +526,6 @@ static cudaError_t attr_pass()
     if constexpr (L <= 10) {
         if ((e = cudaFuncSetAttribute(k_rows3<L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
         if ((e = cudaFuncSetAttribute(k_rows3<L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
-    }
-    if constexpr (L == 7 || L == 8) {
-        if ((e = cudaFuncSetAttribute(k_cols_table<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
-        if ((e = cudaFuncSetAttribute(k_cols_merge_table<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
-    }
-    if constexpr (L == 8) {
-        if ((e = cudaFuncSetAttribute(k_rows_split_table<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
-        if ((e = cudaFuncSetAttribute(k_rows_inv_table<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;
     }
     if constexpr (L >= 7 && L <= 10) {
         if ((e = cudaFuncSetAttribute(k_rows_split<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM)) != cudaSuccess) return e;

@@ -65,10 +65,6 @@ cudaError_t launch_group(int op, int log2a, const FrameDesc* fr, long long count
                          void* scratch, size_t scratch_bytes, cudaStream_t s);
 cudaError_t launch_l2pass_table(int kind, int log2n, const FrameDesc* fr, long long count, const float2* tw,
                                 void* scratch, size_t scratch_bytes, cudaStream_t s);
-cudaError_t launch_r2c_table(int lm, const FrameDesc* fr, long long count, const float2* tw, void* scratch,
-                             size_t scratch_bytes, cudaStream_t s);
-cudaError_t launch_c2r_table(int lm, const FrameDesc* fr, long long count, const float2* tw, void* scratch,
-                             size_t scratch_bytes, cudaStream_t s);
 cudaError_t prepare_groups();
 
 struct LargeDesc {

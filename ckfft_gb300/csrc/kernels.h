@@ -114,9 +114,8 @@ cudaError_t launch_cluster_c2c(bool inverse, int log2n, const void* in, void* ou
 // launch_large_c2c, 128-byte aligned.
 // kind: 0 / 1 complex forward / inverse of 2^log2n points, 2 / 3 real
 // forward / inverse of 2^(log2n+1) points (split / merge fused; dists in
-// complex units).  l2pass_real(kind): the real kind runs on this kernel.
+// complex units).
 bool l2pass_supported(int log2n);
-bool l2pass_real(int kind);
 cudaError_t launch_l2pass(int kind, int log2n, const void* in, void* out, long long count, long long in_dist,
                           long long out_dist, const float2* tw, void* scratch, size_t scratch_bytes,
                           cudaStream_t stream);
